@@ -1,0 +1,37 @@
+"""mak_gb300 -- GB300-native dense orthogonal factorizations (QR, polar, pullbacks).
+
+Python host mirror of the Julia extension: the same entry points and
+algorithm types MatrixAlgebraKit users call, backed by libmak_gb300.so
+(hand-written sm_103a CUDA behind a C ABI).  Bang functions end in ``_``
+(``qr_compact_`` is ``qr_compact!``).
+
+The directory name carries a dot, so load it with::
+
+    import importlib.util, sys
+    spec = importlib.util.spec_from_file_location(
+        "mak_gb300", "<repo>/matrixalgebrakit.jl_gb300/__init__.py",
+        submodule_search_locations=["<repo>/matrixalgebrakit.jl_gb300"])
+    mak = importlib.util.module_from_spec(spec); sys.modules["mak_gb300"] = mak
+    spec.loader.exec_module(mak)
+
+(``__graft_entry__.load_package()`` does exactly this.)
+"""
+
+from . import _lib
+from .algorithms import (ArgumentError, DimensionMismatch, GB300_HouseholderQR,
+                         GB300_PolarNewton, LeftOrthViaPolar, LeftOrthViaQR, default_algorithm,
+                         is_positive, select_algorithm)
+from .qr import (initialize_output, qr_compact, qr_compact_, qr_full, qr_full_, qr_null,
+                 qr_null_)
+
+__all__ = [
+    "ArgumentError", "DimensionMismatch", "GB300_HouseholderQR", "GB300_PolarNewton",
+    "LeftOrthViaQR", "LeftOrthViaPolar", "default_algorithm", "select_algorithm", "is_positive",
+    "qr_compact", "qr_compact_", "qr_full", "qr_full_", "qr_null", "qr_null_",
+    "initialize_output", "library",
+]
+
+
+def library():
+    """The loaded ctypes handle of libmak_gb300.so (raises if unavailable)."""
+    return _lib.load()

@@ -1,0 +1,86 @@
+"""ctypes binding of libmak_gb300.so -- the same C ABI Julia reaches via ``ccall``.
+
+The library is built in-tree by ``build.py``.  There is no CPU fallback: if
+the shared object is missing or fails to load, every entry point raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libmak_gb300.so"
+
+MAK_F64, MAK_C64, MAK_F32, MAK_C32 = 0, 1, 2, 3
+MAK_PREC_NATIVE, MAK_PREC_MIXED = 0, 1
+MAK_OK = 0
+MAK_ERR_CUDA, MAK_ERR_TIMEOUT, MAK_ERR_UNSUPPORTED, MAK_ERR_WORKSPACE = 1000, 1001, 1002, 1003
+
+
+class mak_info(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("rank", C.c_int32),
+                ("converged", C.c_int32), ("residual", C.c_double), ("gauge", C.c_double),
+                ("gauge_atol", C.c_double), ("singular", C.c_int32), ("pad", C.c_int32)]
+
+
+class mak_qr_opts(C.Structure):
+    _fields_ = [("positive", C.c_int32), ("blocksize", C.c_int32), ("precision", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class mak_polar_opts(C.Structure):
+    _fields_ = [("maxiter", C.c_int32), ("precision", C.c_int32), ("tol", C.c_double)]
+
+
+class mak_pullback_opts(C.Structure):
+    _fields_ = [("rank_atol", C.c_double), ("gauge_atol", C.c_double), ("precision", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+_i64 = C.c_int64
+_p = C.c_void_p
+_sz = C.c_size_t
+
+# name -> (restype, argtypes); every symbol declared in include/mak_gb300.h
+SIGNATURES = {
+    "mak_version": (C.c_char_p, []),
+    "mak_status_string": (C.c_char_p, [C.c_int]),
+    "mak_qr_workspace": (C.c_int, [C.c_int, _i64, _i64, C.c_int, C.POINTER(mak_qr_opts),
+                                   C.POINTER(_sz)]),
+}
+_QR_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, C.POINTER(mak_qr_opts), _p, _sz, _p, _p]
+for _kind in ("compact", "full"):
+    for _s in "dzsc":
+        SIGNATURES[f"mak_qr_{_kind}_{_s}"] = (C.c_int, _QR_ARGS)
+
+_lib = None
+_load_error = None
+
+
+def load():
+    """Load the shared library once; raise with the reason if unavailable."""
+    global _lib, _load_error
+    if _lib is not None:
+        return _lib
+    if _load_error is not None:
+        raise RuntimeError(_load_error)
+    path = Path(os.environ.get("MAK_GB300_LIB", LIB_PATH))
+    if not path.exists():
+        _load_error = (f"libmak_gb300.so not found at {path}; build it with "
+                       f"`python -c 'import __graft_entry__ as g; g.build()'` (no CPU fallback exists)")
+        raise RuntimeError(_load_error)
+    lib = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        if not hasattr(lib, name):
+            continue
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def status_string(code: int) -> str:
+    return load().mak_status_string(code).decode()

@@ -1,0 +1,27 @@
+// Internal (C++) interfaces shared between the translation units of
+// libmak_gb300.so.  Each template is explicitly instantiated for double,
+// zcomplex, float and ccomplex in the .cu file that defines it.
+#pragma once
+#include "mak_common.cuh"
+
+namespace mak {
+
+// Blocked Householder QR of A (m x n, destroyed) producing Q (m x qcols,
+// qcols = min(m,n) compact or m full) and optionally R (rrows x n).
+// Workspace from `ar`; with ar.base == nullptr only sizes are accumulated.
+template <class T>
+int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64_t ldq,
+           int64_t qcols, T* R, int64_t ldr, int64_t rrows, int positive, int blocksize,
+           int precision, Arena& ar, mak_info* info);
+
+// In-place inverse of the n x n matrix X (Gauss-Jordan with partial
+// pivoting).  On return X holds inv(P X) where P is the row permutation;
+// `iperm` (n ints) receives the inverse permutation so that
+// inv(X)[:, c] = Xout[:, iperm[c]].
+template <class T>
+int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int precision,
+                Arena& ar, mak_info* info);
+
+int info_reset(cudaStream_t st, mak_info* info);
+
+}  // namespace mak

@@ -1,0 +1,239 @@
+// Shared device/host helpers for the GB300 orthogonal-factorization library.
+//
+// Scalar model: the four LAPACK element types Float64 (d), ComplexF64 (z),
+// Float32 (s), ComplexF32 (c); complex values are stored interleaved
+// (re, im) exactly like Julia's ComplexF64/ComplexF32 and C99 complex, so a
+// CuMatrix{ComplexF64} pointer can be passed straight through the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#include "../../include/mak_gb300.h"
+
+namespace mak {
+
+// ------------------------------------------------------------ complex type --
+template <class R>
+struct __align__(2 * sizeof(R)) cplx {
+  R re, im;
+  __host__ __device__ cplx() {}
+  __host__ __device__ constexpr cplx(R r) : re(r), im(0) {}
+  __host__ __device__ constexpr cplx(R r, R i) : re(r), im(i) {}
+};
+template <class R> __host__ __device__ __forceinline__ cplx<R> operator+(cplx<R> a, cplx<R> b) { return {a.re + b.re, a.im + b.im}; }
+template <class R> __host__ __device__ __forceinline__ cplx<R> operator-(cplx<R> a, cplx<R> b) { return {a.re - b.re, a.im - b.im}; }
+template <class R> __host__ __device__ __forceinline__ cplx<R> operator-(cplx<R> a) { return {-a.re, -a.im}; }
+template <class R> __host__ __device__ __forceinline__ cplx<R> operator*(cplx<R> a, cplx<R> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <class R> __host__ __device__ __forceinline__ cplx<R> operator*(R s, cplx<R> a) { return {s * a.re, s * a.im}; }
+template <class R> __host__ __device__ __forceinline__ cplx<R> operator*(cplx<R> a, R s) { return {s * a.re, s * a.im}; }
+template <class R> __host__ __device__ __forceinline__ cplx<R>& operator+=(cplx<R>& a, cplx<R> b) { a.re += b.re; a.im += b.im; return a; }
+template <class R> __host__ __device__ __forceinline__ cplx<R>& operator-=(cplx<R>& a, cplx<R> b) { a.re -= b.re; a.im -= b.im; return a; }
+template <class R> __host__ __device__ __forceinline__ bool operator==(cplx<R> a, cplx<R> b) { return a.re == b.re && a.im == b.im; }
+
+using zcomplex = cplx<double>;
+using ccomplex = cplx<float>;
+
+// ------------------------------------------------------------ scalar traits --
+template <class T> struct traits;
+template <> struct traits<double> { using real = double; static constexpr bool cpx = false; static constexpr int code = MAK_F64; };
+template <> struct traits<float>  { using real = float;  static constexpr bool cpx = false; static constexpr int code = MAK_F32; };
+template <> struct traits<zcomplex> { using real = double; static constexpr bool cpx = true; static constexpr int code = MAK_C64; };
+template <> struct traits<ccomplex> { using real = float;  static constexpr bool cpx = true; static constexpr int code = MAK_C32; };
+template <class T> using real_t = typename traits<T>::real;
+
+__host__ __device__ __forceinline__ double conj_(double x) { return x; }
+__host__ __device__ __forceinline__ float conj_(float x) { return x; }
+template <class R> __host__ __device__ __forceinline__ cplx<R> conj_(cplx<R> x) { return {x.re, -x.im}; }
+
+__host__ __device__ __forceinline__ double re_(double x) { return x; }
+__host__ __device__ __forceinline__ float re_(float x) { return x; }
+template <class R> __host__ __device__ __forceinline__ R re_(cplx<R> x) { return x.re; }
+__host__ __device__ __forceinline__ double im_(double) { return 0.0; }
+__host__ __device__ __forceinline__ float im_(float) { return 0.0f; }
+template <class R> __host__ __device__ __forceinline__ R im_(cplx<R> x) { return x.im; }
+
+__host__ __device__ __forceinline__ double abs2_(double x) { return x * x; }
+__host__ __device__ __forceinline__ float abs2_(float x) { return x * x; }
+template <class R> __host__ __device__ __forceinline__ R abs2_(cplx<R> x) { return x.re * x.re + x.im * x.im; }
+
+__host__ __device__ __forceinline__ double abs_(double x) { return fabs(x); }
+__host__ __device__ __forceinline__ float abs_(float x) { return fabsf(x); }
+__host__ __device__ __forceinline__ double abs_(cplx<double> x) { return hypot(x.re, x.im); }
+__host__ __device__ __forceinline__ float abs_(cplx<float> x) { return hypotf(x.re, x.im); }
+
+// fused multiply-add  acc + a*b
+__device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+template <class R> __device__ __forceinline__ cplx<R> fma_(cplx<R> a, cplx<R> b, cplx<R> c) {
+  cplx<R> r;
+  r.re = fma_(a.re, b.re, fma_(-a.im, b.im, c.re));
+  r.im = fma_(a.re, b.im, fma_(a.im, b.re, c.im));
+  return r;
+}
+
+template <class T> __host__ __device__ __forceinline__ T make_scalar(real_t<T> re, real_t<T> im);
+template <> __host__ __device__ __forceinline__ double make_scalar<double>(double re, double) { return re; }
+template <> __host__ __device__ __forceinline__ float make_scalar<float>(float re, float) { return re; }
+template <> __host__ __device__ __forceinline__ zcomplex make_scalar<zcomplex>(double re, double im) { return {re, im}; }
+template <> __host__ __device__ __forceinline__ ccomplex make_scalar<ccomplex>(float re, float im) { return {re, im}; }
+
+template <class T> __host__ __device__ __forceinline__ T zero_() { return make_scalar<T>(0, 0); }
+template <class T> __host__ __device__ __forceinline__ T one_() { return make_scalar<T>(1, 0); }
+
+// multiplicative inverse of a scalar (complex: Smith-free plain formula with
+// a single real division, adequate for the non-tiny values it is used on)
+__device__ __forceinline__ double inv_(double x) { return 1.0 / x; }
+__device__ __forceinline__ float inv_(float x) { return 1.0f / x; }
+template <class R> __device__ __forceinline__ cplx<R> inv_(cplx<R> x) {
+  R s = fabs(x.re) > fabs(x.im) ? fabs(x.re) : fabs(x.im);
+  if (s == R(0)) return {R(1) / s, R(0)};
+  R xr = x.re / s, xi = x.im / s;
+  R d = (xr * xr + xi * xi) * s;
+  return {xr / d, -xi / d};
+}
+
+// sign_safe (reference src/common/safemethods.jl:10-11):
+// real: s < 0 ? -1 : +1 ; complex: s/|s| with 0 -> 1
+__device__ __forceinline__ double sign_safe_(double s) { return s < 0.0 ? -1.0 : 1.0; }
+__device__ __forceinline__ float sign_safe_(float s) { return s < 0.0f ? -1.0f : 1.0f; }
+template <class R> __device__ __forceinline__ cplx<R> sign_safe_(cplx<R> s) {
+  if (s.re == R(0) && s.im == R(0)) return {R(1), R(0)};
+  R a = abs_(s);
+  return {s.re / a, s.im / a};
+}
+
+// L1-bypassing loads for values written by other CTAs of the same launch
+// (after a grid barrier); L1 is not coherent across SMs.
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ zcomplex ld_cg(const zcomplex* p) {
+  double2 v = __ldcg((const double2*)p);
+  return {v.x, v.y};
+}
+__device__ __forceinline__ ccomplex ld_cg(const ccomplex* p) {
+  float2 v = __ldcg((const float2*)p);
+  return {v.x, v.y};
+}
+__device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }
+
+// ------------------------------------------------------------ warp helpers --
+__device__ __forceinline__ double shfl_xor_(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ float shfl_xor_(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+template <class R> __device__ __forceinline__ cplx<R> shfl_xor_(cplx<R> v, int m) {
+  return {shfl_xor_(v.re, m), shfl_xor_(v.im, m)};
+}
+template <class T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) v += shfl_xor_(v, m);
+  return v;
+}
+template <class R> __device__ __forceinline__ R warp_max(R v) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) { R o = shfl_xor_(v, m); v = o > v ? o : v; }
+  return v;
+}
+
+// Block-wide reductions (deterministic: fixed shuffle tree, fixed warp order).
+// `sh` must hold 32 elements; every thread receives the result.
+template <class T>
+__device__ __forceinline__ T block_sum(T v, T* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  T r = zero_<T>();
+  for (int w = 0; w < nw; w++) r += sh[w];
+  return r;
+}
+template <class R>
+__device__ __forceinline__ R block_max(R v, R* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  R r = sh[0];
+  for (int w = 1; w < nw; w++) r = sh[w] > r ? sh[w] : r;
+  return r;
+}
+
+// ------------------------------------------------------ bounded grid barrier --
+// Used only inside cooperative launches (all CTAs are guaranteed co-resident).
+// Every wait is bounded: after kSpinLimit polls the CTA records
+// MAK_ERR_TIMEOUT in *status and the barrier reports failure, so a kernel can
+// never hang the GPU.  `bar[0]` counts arrivals, `bar[1]` is the generation.
+constexpr long long kSpinLimit = 1ll << 22;  // x >=64 ns sleep -> well under a minute
+
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    if (nblocks > 1) {
+      volatile unsigned* vgen = bar + 1;
+      unsigned g = *vgen;
+      __threadfence();
+      unsigned arrived = atomicAdd(bar, 1u);
+      if (arrived == nblocks - 1) {
+        atomicExch(bar, 0u);
+        __threadfence();
+        atomicAdd(bar + 1, 1u);
+      } else {
+        long long spins = 0;
+        while (*vgen == g) {
+          if (++spins > kSpinLimit) { atomicExch(status, MAK_ERR_TIMEOUT); ok = 0; break; }
+          if (*((volatile int*)status) == MAK_ERR_TIMEOUT) { ok = 0; break; }
+          __nanosleep(64);
+        }
+      }
+      __threadfence();
+    }
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// --------------------------------------------------------------- host side --
+#define MAK_CUDA_TRY(expr)                         \
+  do {                                             \
+    cudaError_t e_ = (expr);                       \
+    if (e_ != cudaSuccess) return MAK_ERR_CUDA;    \
+  } while (0)
+
+#define MAK_TRY(expr)          \
+  do {                         \
+    int r_ = (expr);           \
+    if (r_ != 0) return r_;    \
+  } while (0)
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Bump allocator over the caller's workspace.  With base == nullptr it only
+// measures (used by the *_workspace queries, LAPACK's lwork = -1 pattern).
+struct Arena {
+  char* base;
+  size_t cap;
+  size_t off = 0;
+  Arena(void* b, size_t c) : base((char*)b), cap(c) {}
+  template <class T>
+  T* take(size_t count) {
+    // align the absolute address (offsets alone when only measuring)
+    size_t addr = (size_t)base + off;
+    off += align_up(addr, 256) - addr;
+    T* p = base ? (T*)(base + off) : nullptr;
+    off += count * sizeof(T);
+    return p;
+  }
+  bool ok() const { return base == nullptr || off <= cap; }
+};
+
+int num_sms();
+int max_smem_optin();
+
+}  // namespace mak

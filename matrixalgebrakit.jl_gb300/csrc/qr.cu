@@ -1,0 +1,594 @@
+// Blocked Householder QR with positive-diagonal gauge, GB300 native.
+//
+// Replaces the reference's LAPACK/cuSOLVER path
+//   qr_householder!  (src/implementations/qr.jl:132-188)
+//   = geqrt!/geqrf!  (panel + T factor, src/yalapack.jl:303-333 / 168-199)
+//   + gemqrt!/unmqr! on one!(Q)  (Q formation, src/yalapack.jl:882-927)
+//   + uppertriangular! R copy   (src/common/initialization.jl:18-26)
+//   + gaugefix!(qr_householder!) (src/common/gauge.jl:16-25, sign_safe
+//     src/common/safemethods.jl:10-11)
+//
+// Structure on the device, per panel of jb <= 32 columns starting at j0:
+//  1. qr_panel_kernel: ONE cooperative launch factors the (m-j0) x jb panel.
+//     Each CTA keeps a contiguous slab of panel rows resident in shared
+//     memory for the whole panel; a column costs two bounded grid barriers
+//     (reflector norm, then the w = v^H A row vector).  Norms are overflow
+//     safe (scaled sum of squares) and every cross-CTA reduction is done in
+//     a fixed order, so all CTAs derive bit-identical beta/tau.  The panel's
+//     Gram matrix V^H V is reduced at the end and CTA 0 forms the T factor
+//     (forward, column-wise larft recurrence).
+//  2. larfb on the trailing columns:  W = V^H C (split-K GEMM, V read in
+//     place through a unit-lower mask), W2 = T^H W (reduce_trmm_kernel),
+//     C -= V W2 (GEMM).
+// Q is then accumulated backwards (orgqr order, exploiting the identity
+// structure: block b only touches Q[j0:, j0:]) starting from [diag(s); 0]
+// where s = sign_safe(diag R): the gauge fix Q <- Q diag(s) is folded into the
+// starting matrix because Q diag(s) = H_1...H_k [diag(s); 0].  R is written
+// once, already multiplied by conj(s) row-wise.
+#include "gemm.cuh"
+#include "internal.h"
+
+#include <mutex>
+
+namespace mak {
+
+constexpr int NBMAX = 32;      // widest panel handled by one cooperative launch
+constexpr int PANEL_THREADS = 256;
+
+template <class T>
+struct PanelArgs {
+  T* A;                 // panel (row j0, col j0) of the packed matrix
+  int64_t lda;
+  int mp;               // panel rows
+  int jb;               // panel columns
+  int rpc;              // panel rows owned by one CTA
+  T* tau;               // [jb]
+  T* Tm;                // [NBMAX x NBMAX], ld NBMAX
+  real_t<T>* part_nrm;  // [G][2]  (scale, scaled sum of squares)
+  T* part_w;            // [G][NBMAX]
+  T* part_g;            // [G][NBMAX*NBMAX]
+  T* alpha_buf;         // [NBMAX]
+  unsigned* bar;        // grid barrier words
+  int* status;
+};
+
+// beta / tau / 1/(alpha-beta) of one reflector, LAPACK ?larfg convention:
+// H^H [alpha; x] = [beta; 0], H = I - tau v v^H, v = [1; x/(alpha-beta)].
+template <class T>
+__device__ void larfg_scalars(T alpha, real_t<T> xnorm, T& beta, T& tau, T& scal) {
+  using R = real_t<T>;
+  R ar = re_(alpha), ai = im_(alpha);
+  if (xnorm == R(0) && ai == R(0)) {
+    tau = zero_<T>();
+    beta = alpha;
+    scal = one_<T>();
+    return;
+  }
+  R w = fmax(fmax(fabs(ar), fabs(ai)), xnorm);
+  R nrm = w * sqrt((ar / w) * (ar / w) + (ai / w) * (ai / w) + (xnorm / w) * (xnorm / w));
+  R b = ar >= R(0) ? -nrm : nrm;
+  beta = make_scalar<T>(b, 0);
+  tau = make_scalar<T>((b - ar) / b, -ai / b);
+  scal = inv_(alpha - beta);
+}
+
+template <class T>
+__global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a) {
+  using R = real_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x jb, column-major, ld = rpc
+  __shared__ R red_r[32];
+  __shared__ T red_t[32];
+  __shared__ T wsh[NBMAX];
+  __shared__ T sc[3];
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  const int rpc = a.rpc, jb = a.jb;
+  const int r0 = b * rpc;
+  const int nr = max(0, min(a.mp, r0 + rpc) - r0);
+
+  for (int c = 0; c < jb; c++)
+    for (int r = tid; r < nr; r += blockDim.x) Ps[r + c * rpc] = a.A[(r0 + r) + (int64_t)c * a.lda];
+  __syncthreads();
+
+  for (int j = 0; j < jb; j++) {
+    T* col = Ps + j * rpc;
+    // ---- phase A: scaled sum of squares of x = column j below the diagonal
+    const int rs = max(0, j + 1 - r0);
+    R mx = R(0);
+    for (int r = rs + tid; r < nr; r += blockDim.x) mx = fmax(mx, abs_(col[r]));
+    mx = block_max(mx, red_r);
+    R ssq = R(0);
+    if (mx > R(0)) {
+      R inv = R(1) / mx;
+      for (int r = rs + tid; r < nr; r += blockDim.x) ssq += abs2_(col[r] * inv);
+    }
+    ssq = block_sum(ssq, red_r);
+    if (tid == 0) {
+      a.part_nrm[2 * b] = mx;
+      a.part_nrm[2 * b + 1] = ssq;
+      if (j >= r0 && j < r0 + nr) a.alpha_buf[j] = col[j - r0];
+    }
+    if (!grid_barrier(a.bar, G, a.status)) return;
+
+    // ---- phase B: every CTA derives the same beta/tau from the partials
+    if (wid == 0) {
+      R m = R(0);
+      for (int q = lane; q < G; q += 32) m = fmax(m, ld_cg(&a.part_nrm[2 * q]));
+      m = warp_max(m);
+      R s = R(0);
+      if (m > R(0)) {
+        for (int q = lane; q < G; q += 32) {
+          R sq = ld_cg(&a.part_nrm[2 * q]);
+          if (sq > R(0)) {
+            R t = sq / m;
+            s += ld_cg(&a.part_nrm[2 * q + 1]) * t * t;
+          }
+        }
+      }
+      s = warp_sum(s);
+      if (lane == 0) {
+        R xnorm = m * sqrt(s);
+        T alpha = ld_cg(&a.alpha_buf[j]);
+        T beta, tau, scal;
+        larfg_scalars(alpha, xnorm, beta, tau, scal);
+        sc[0] = beta;
+        sc[1] = tau;
+        sc[2] = scal;
+      }
+    }
+    __syncthreads();
+    const T beta = sc[0], tau = sc[1], scal = sc[2];
+    if (b == 0 && tid == 0) a.tau[j] = tau;
+    for (int r = rs + tid; r < nr; r += blockDim.x) col[r] = col[r] * scal;
+    if (tid == 0 && j >= r0 && j < r0 + nr) col[j - r0] = beta;
+    __syncthreads();
+    if (j + 1 >= jb) break;
+
+    // partial w_c = sum_{r >= j} conj(v_r) A[r, c], c > j  (v_j = 1)
+    const int rj = max(0, j - r0);
+    for (int c = j + 1 + wid; c < jb; c += nw) {
+      T s = zero_<T>();
+      for (int r = rj + lane; r < nr; r += 32) {
+        T v = (r0 + r == j) ? one_<T>() : col[r];
+        s = fma_(conj_(v), Ps[r + c * rpc], s);
+      }
+      s = warp_sum(s);
+      if (lane == 0) a.part_w[b * NBMAX + c] = s;
+    }
+    if (!grid_barrier(a.bar, G, a.status)) return;
+
+    // ---- phase C: combine w in a fixed order, apply H_j^H to columns > j
+    for (int c = j + 1 + wid; c < jb; c += nw) {
+      T s = zero_<T>();
+      for (int q = lane; q < G; q += 32) s += ld_cg(&a.part_w[q * NBMAX + c]);
+      s = warp_sum(s);
+      if (lane == 0) wsh[c] = s;
+    }
+    __syncthreads();
+    const T ctau = conj_(tau);
+    for (int c = j + 1; c < jb; c++) {
+      const T f = ctau * wsh[c];
+      T* pc = Ps + c * rpc;
+      for (int r = rj + tid; r < nr; r += blockDim.x) {
+        T v = (r0 + r == j) ? one_<T>() : col[r];
+        pc[r] -= v * f;
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- Gram partials of V (unit lower trapezoidal) for the T factor
+  for (int pr = wid; pr < jb * jb; pr += nw) {
+    const int i = pr % jb, jj = pr / jb;
+    if (i >= jj) continue;
+    T s = zero_<T>();
+    const int rb = max(0, i - r0);
+    for (int r = rb + lane; r < nr; r += 32) {
+      const int gr = r0 + r;
+      T vi = (gr == i) ? one_<T>() : Ps[r + i * rpc];
+      T vj = (gr == jj) ? one_<T>() : (gr > jj ? Ps[r + jj * rpc] : zero_<T>());
+      s = fma_(conj_(vi), vj, s);
+    }
+    s = warp_sum(s);
+    if (lane == 0) a.part_g[(int64_t)b * NBMAX * NBMAX + i + jj * NBMAX] = s;
+  }
+  for (int c = 0; c < jb; c++)
+    for (int r = tid; r < nr; r += blockDim.x) a.A[(r0 + r) + (int64_t)c * a.lda] = Ps[r + c * rpc];
+  if (!grid_barrier(a.bar, G, a.status)) return;
+  if (b != 0) return;
+
+  // ---- CTA 0: T factor, larft forward column-wise recurrence
+  __shared__ T gram[NBMAX][NBMAX + 1];
+  __shared__ T tt[NBMAX][NBMAX + 1];
+  __shared__ T tv[NBMAX];
+  for (int pr = tid; pr < jb * jb; pr += blockDim.x) {
+    const int i = pr % jb, jj = pr / jb;
+    T s = zero_<T>();
+    if (i < jj)
+      for (int q = 0; q < G; q++) s += ld_cg(&a.part_g[(int64_t)q * NBMAX * NBMAX + i + jj * NBMAX]);
+    gram[i][jj] = s;
+    tt[i][jj] = zero_<T>();
+  }
+  __syncthreads();
+  for (int jj = 0; jj < jb; jj++) {
+    const T tj = a.tau[jj];
+    if (tid < jj) tv[tid] = -(tj * gram[tid][jj]);
+    __syncthreads();
+    if (tid < jj) {
+      T s = zero_<T>();
+      for (int l = tid; l < jj; l++) s = fma_(tt[tid][l], tv[l], s);
+      tt[tid][jj] = s;
+    }
+    if (tid == 0) tt[jj][jj] = tj;
+    __syncthreads();
+  }
+  for (int pr = tid; pr < NBMAX * NBMAX; pr += blockDim.x) {
+    const int i = pr % NBMAX, jj = pr / NBMAX;
+    a.Tm[i + jj * NBMAX] = (i < jb && jj < jb) ? tt[i][jj] : zero_<T>();
+  }
+}
+
+// W2[:, c] = op(Tm) * sum_s Wpart[s][:, c]   (op = ^H for the factorization,
+// identity for Q formation).  Fixed summation order -> deterministic.
+template <class T>
+__global__ void __launch_bounds__(256) reduce_trmm_kernel(int jb, int nt, int splits,
+                                                          const T* __restrict__ Wpart,
+                                                          int64_t sstride,
+                                                          const T* __restrict__ Tm, int conjtrans,
+                                                          T* __restrict__ W2) {
+  __shared__ T Ts[NBMAX][NBMAX + 1];
+  __shared__ T Ws[NBMAX][33];
+  const int c0 = blockIdx.x * 32;
+  for (int e = threadIdx.x; e < jb * jb; e += blockDim.x) {
+    const int i = e % jb, l = e / jb;
+    Ts[i][l] = conjtrans ? conj_(Tm[l + i * NBMAX]) : Tm[i + l * NBMAX];
+  }
+  for (int e = threadIdx.x; e < jb * 32; e += blockDim.x) {
+    const int i = e % jb, cc = e / jb;
+    T s = zero_<T>();
+    if (c0 + cc < nt)
+      for (int q = 0; q < splits; q++) s += Wpart[q * sstride + i + (int64_t)(c0 + cc) * jb];
+    Ws[i][cc] = s;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < jb * 32; e += blockDim.x) {
+    const int i = e % jb, cc = e / jb;
+    if (c0 + cc >= nt) continue;
+    T s = zero_<T>();
+    for (int l = 0; l < jb; l++) s = fma_(Ts[i][l], Ws[l][cc], s);
+    W2[i + (int64_t)(c0 + cc) * jb] = s;
+  }
+}
+
+template <class T>
+__global__ void signs_kernel(int k, const T* A, int64_t lda, int positive, T* s) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < k) s[j] = positive ? sign_safe_(A[j + j * lda]) : one_<T>();
+}
+
+// R[i, j] = (i <= j && i < k) ? conj(s_i) A[i, j] : 0   for i < rrows, j < n
+template <class T>
+__global__ void extract_r_kernel(int64_t rrows, int64_t n, int64_t k, const T* A, int64_t lda,
+                                 const T* s, T* R, int64_t ldr) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t j = blockIdx.y;
+  for (; j < n; j += gridDim.y) {
+    if (i >= rrows) return;
+    T v = zero_<T>();
+    if (i <= j && i < k) v = conj_(s[i]) * A[i + j * lda];
+    R[i + j * ldr] = v;
+  }
+}
+
+// Q = [diag(s); 0] on the first k columns, identity beyond (qr_full)
+template <class T>
+__global__ void init_q_kernel(int64_t m, int64_t qcols, int64_t k, const T* s, T* Q, int64_t ldq) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t j = blockIdx.y; j < qcols; j += gridDim.y) {
+    if (i >= m) return;
+    T v = zero_<T>();
+    if (i == j) v = (j < k) ? s[j] : one_<T>();
+    Q[i + j * ldq] = v;
+  }
+}
+
+__global__ void info_reset_kernel(mak_info* info) {
+  info->status = 0;
+  info->iterations = 0;
+  info->rank = 0;
+  info->converged = 0;
+  info->residual = 0.0;
+  info->gauge = 0.0;
+  info->gauge_atol = 0.0;
+  info->singular = 0;
+  info->pad = 0;
+}
+
+int info_reset(cudaStream_t st, mak_info* info) {
+  info_reset_kernel<<<1, 1, 0, st>>>(info);
+  return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+}
+
+int num_sms() {
+  static int v = 0;
+  static std::once_flag f;
+  std::call_once(f, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    if (v <= 0) v = 152;
+  });
+  return v;
+}
+int max_smem_optin() {
+  static int v = 0;
+  static std::once_flag f;
+  std::call_once(f, [] {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (v <= 0) v = 227 * 1024;
+  });
+  return v;
+}
+
+// Shared memory available to the panel slab: the opt-in maximum minus the
+// kernel's static shared memory (T-factor scratch), queried once per type.
+template <class T>
+static size_t panel_slab_cap() {
+  static size_t cap = 0;
+  static std::once_flag f;
+  std::call_once(f, [] {
+    cudaFuncAttributes fa;
+    size_t stat = 48 * 1024;
+    if (cudaFuncGetAttributes(&fa, qr_panel_kernel<T>) == cudaSuccess) stat = fa.sharedSizeBytes;
+    cap = (size_t)max_smem_optin() - stat - 1024;
+    cudaFuncSetAttribute(qr_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cap);
+  });
+  return cap;
+}
+
+// Grid shape of the panel kernel: rows per CTA bounded below by 64 (a grid
+// barrier is only paid when there is real parallel work) and above by the
+// shared-memory slab size; at most one CTA per SM (cooperative launch).
+struct PanelShape {
+  int G, rpc;
+  size_t smem;
+};
+template <class T>
+static int panel_shape(int64_t mp, int jb, PanelShape& ps) {
+  const int max_ctas = num_sms();
+  const size_t cap = panel_slab_cap<T>();
+  int64_t rpc_max = (int64_t)(cap / ((size_t)jb * sizeof(T)));
+  int64_t G = ceil_div(mp, 64);
+  if (G > max_ctas) G = max_ctas;
+  if (G < 1) G = 1;
+  int64_t rpc = ceil_div(mp, G);
+  if (rpc > rpc_max) {
+    G = ceil_div(mp, rpc_max);
+    if (G > max_ctas) return MAK_ERR_UNSUPPORTED;
+    rpc = ceil_div(mp, G);
+  }
+  if (rpc < 1) rpc = 1;
+  G = ceil_div(mp, rpc);
+  if (G < 1) G = 1;
+  ps.G = (int)G;
+  ps.rpc = (int)rpc;
+  ps.smem = (size_t)ps.rpc * jb * sizeof(T);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_panel_kernel<T>, PANEL_THREADS,
+                                                    ps.smem) != cudaSuccess)
+    return MAK_ERR_CUDA;
+  if ((int64_t)per_sm * max_ctas < G) return MAK_ERR_UNSUPPORTED;
+  return 0;
+}
+
+template <class T>
+int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64_t ldq,
+           int64_t qcols, T* R, int64_t ldr, int64_t rrows, int positive, int blocksize,
+           int precision, Arena& ar, mak_info* info) {
+  (void)precision;
+  const int64_t k = m < n ? m : n;
+  const int nb = (blocksize > 0 && blocksize < NBMAX) ? blocksize : NBMAX;
+  const int64_t nblk = ceil_div(k, nb);
+  const int64_t wmax = (n > qcols ? n : qcols);
+  const int sms = num_sms();
+  const int gmax = sms;  // upper bound on panel CTAs (for workspace sizing)
+  const int max_splits = 64;
+
+  T* tau = ar.take<T>(k > 0 ? k : 1);
+  T* Ts = ar.take<T>((size_t)(nblk > 0 ? nblk : 1) * NBMAX * NBMAX);
+  T* sgn = ar.take<T>(k > 0 ? k : 1);
+  T* Wpart = ar.take<T>((size_t)max_splits * nb * (wmax > 0 ? wmax : 1));
+  T* W2 = ar.take<T>((size_t)nb * (wmax > 0 ? wmax : 1));
+  real_t<T>* part_nrm = ar.take<real_t<T>>((size_t)2 * gmax);
+  T* part_w = ar.take<T>((size_t)gmax * NBMAX);
+  T* part_g = ar.take<T>((size_t)gmax * NBMAX * NBMAX);
+  T* alpha_buf = ar.take<T>(NBMAX);
+  unsigned* bar = ar.take<unsigned>(2);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  int* status = &info->status;
+
+  MAK_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+
+  // ------------------------------------------------------------ factor
+  for (int64_t j0 = 0; j0 < k; j0 += nb) {
+    const int jb = (int)((k - j0) < nb ? (k - j0) : nb);
+    const int64_t mp = m - j0;
+    T* Ap = A + j0 + j0 * lda;
+    T* Tb = Ts + (j0 / nb) * NBMAX * NBMAX;
+    PanelShape ps;
+    MAK_TRY(panel_shape<T>(mp, jb, ps));
+    PanelArgs<T> pa{Ap, lda, (int)mp, jb, ps.rpc, tau + j0, Tb, part_nrm, part_w,
+                    part_g, alpha_buf, bar, status};
+    void* args[] = {&pa};
+    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)qr_panel_kernel<T>, dim3(ps.G),
+                                             dim3(PANEL_THREADS), args, ps.smem, st));
+    const int64_t nt = n - j0 - jb;
+    if (nt > 0) {
+      T* C = A + j0 + (j0 + jb) * lda;
+      int splits = pick_splits(jb, nt, mp, sms);
+      if (splits > max_splits) splits = max_splits;
+      int used = 1;
+      MAK_TRY(gemm<T>(st, jb, nt, mp, one_<T>(), opnd<T>(Ap, lda, OP_C, MASK_UNIT_LOWER),
+                      opnd<T>(C, lda), zero_<T>(), Wpart, jb, splits, (int64_t)jb * nt, &used));
+      reduce_trmm_kernel<T><<<(unsigned)ceil_div(nt, 32), 256, 0, st>>>(
+          jb, (int)nt, used, Wpart, (int64_t)jb * nt, Tb, 1, W2);
+      MAK_CUDA_TRY(cudaGetLastError());
+      MAK_TRY(gemm<T>(st, mp, nt, jb, -one_<T>(), opnd<T>(Ap, lda, OP_N, MASK_UNIT_LOWER),
+                      opnd<T>(W2, jb), one_<T>(), C, lda));
+    }
+  }
+
+  // ------------------------------------------------------ R and the gauge
+  if (k > 0) {
+    signs_kernel<T><<<(unsigned)ceil_div(k, 256), 256, 0, st>>>((int)k, A, lda, positive, sgn);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
+  if (R != nullptr && rrows > 0 && n > 0) {
+    dim3 g((unsigned)ceil_div(rrows, 256), (unsigned)(n < 65535 ? n : 65535));
+    extract_r_kernel<T><<<g, 256, 0, st>>>(rrows, n, k, A, lda, sgn, R, ldr);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
+  if (m > 0 && qcols > 0) {
+    dim3 g((unsigned)ceil_div(m, 256), (unsigned)(qcols < 65535 ? qcols : 65535));
+    init_q_kernel<T><<<g, 256, 0, st>>>(m, qcols, k, sgn, Q, ldq);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
+
+  // ------------------------------------------- Q = H_1 ... H_k [diag(s); 0]
+  for (int64_t bi = nblk - 1; bi >= 0; bi--) {
+    const int64_t j0 = bi * nb;
+    const int jb = (int)((k - j0) < nb ? (k - j0) : nb);
+    const int64_t mp = m - j0;
+    const int64_t qt = qcols - j0;
+    if (qt <= 0) continue;
+    const T* Ap = A + j0 + j0 * lda;
+    const T* Tb = Ts + bi * NBMAX * NBMAX;
+    T* Qs = Q + j0 + j0 * ldq;
+    int splits = pick_splits(jb, qt, mp, sms);
+    if (splits > max_splits) splits = max_splits;
+    int used = 1;
+    MAK_TRY(gemm<T>(st, jb, qt, mp, one_<T>(), opnd<T>(Ap, lda, OP_C, MASK_UNIT_LOWER),
+                    opnd<T>(Qs, ldq), zero_<T>(), Wpart, jb, splits, (int64_t)jb * qt, &used));
+    reduce_trmm_kernel<T><<<(unsigned)ceil_div(qt, 32), 256, 0, st>>>(
+        jb, (int)qt, used, Wpart, (int64_t)jb * qt, Tb, 0, W2);
+    MAK_CUDA_TRY(cudaGetLastError());
+    MAK_TRY(gemm<T>(st, mp, qt, jb, -one_<T>(), opnd<T>(Ap, lda, OP_N, MASK_UNIT_LOWER),
+                    opnd<T>(W2, jb), one_<T>(), Qs, ldq));
+  }
+  return 0;
+}
+
+#define MAK_INST_QR(T)                                                                        \
+  template int qr_run<T>(cudaStream_t, int64_t, int64_t, T*, int64_t, T*, int64_t, int64_t, \
+                         T*, int64_t, int64_t, int, int, int, Arena&, mak_info*);
+MAK_INST_QR(double)
+MAK_INST_QR(float)
+MAK_INST_QR(zcomplex)
+MAK_INST_QR(ccomplex)
+
+// ------------------------------------------------------------ C entry ---
+
+template <class T>
+static int qr_entry(int full, int64_t m, int64_t n, void* Av, int64_t lda, void* Qv, int64_t ldq,
+                    void* Rv, int64_t ldr, const mak_qr_opts* opts, void* work, size_t work_bytes,
+                    mak_info* info, mak_stream_t stream) {
+  T* A = (T*)Av;
+  T* Q = (T*)Qv;
+  T* R = (T*)Rv;
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  const int64_t k = m < n ? m : n;
+  const int64_t qcols = full ? m : k;
+  const int64_t rrows = full ? m : k;
+  if (A == nullptr && m * n > 0) return -3;
+  if (lda < (m > 1 ? m : 1)) return -4;
+  if (Q == nullptr && m * qcols > 0) return -5;
+  if (Q != nullptr && (void*)Q == (void*)A) return -5;  // in-place Q is not provided
+  if (ldq < (m > 1 ? m : 1)) return -6;
+  if (R != nullptr && ldr < (rrows > 1 ? rrows : 1)) return -8;
+  mak_qr_opts o{1, 0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.blocksize < 0 || o.blocksize > NBMAX) return -9;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -9;
+  cudaStream_t st = (cudaStream_t)stream;
+  Arena ar(work, work_bytes);
+  mak_info* inf = info ? info : ar.take<mak_info>(1);
+  if (work == nullptr && info == nullptr) return -11;
+  // size check first (a measuring pass)
+  {
+    Arena meas(nullptr, 0);
+    if (!info) meas.take<mak_info>(1);
+    qr_run<T>(st, m, n, nullptr, lda, nullptr, ldq, qcols, nullptr, ldr, rrows, o.positive,
+              o.blocksize, o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -12;
+  }
+  MAK_TRY(info_reset(st, inf));
+  return qr_run<T>(st, m, n, A, lda, Q, ldq, qcols, R, ldr, rrows, o.positive, o.blocksize,
+                   o.precision, ar, inf);
+}
+
+}  // namespace mak
+
+using namespace mak;
+
+extern "C" {
+
+int mak_qr_workspace(int dtype, int64_t m, int64_t n, int full, const mak_qr_opts* opts,
+                     size_t* bytes) {
+  if (bytes == nullptr) return -6;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  mak_qr_opts o{1, 0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  const int64_t k = m < n ? m : n;
+  const int64_t qcols = full ? m : k;
+  const int64_t rrows = full ? m : k;
+  Arena meas(nullptr, 0);
+  meas.take<mak_info>(1);
+  switch (dtype) {
+    case MAK_F64: qr_run<double>(0, m, n, nullptr, m, nullptr, m, qcols, nullptr, rrows, rrows, o.positive, o.blocksize, o.precision, meas, nullptr); break;
+    case MAK_C64: qr_run<zcomplex>(0, m, n, nullptr, m, nullptr, m, qcols, nullptr, rrows, rrows, o.positive, o.blocksize, o.precision, meas, nullptr); break;
+    case MAK_F32: qr_run<float>(0, m, n, nullptr, m, nullptr, m, qcols, nullptr, rrows, rrows, o.positive, o.blocksize, o.precision, meas, nullptr); break;
+    case MAK_C32: qr_run<ccomplex>(0, m, n, nullptr, m, nullptr, m, qcols, nullptr, rrows, rrows, o.positive, o.blocksize, o.precision, meas, nullptr); break;
+    default: return -1;
+  }
+  *bytes = meas.off + 256;
+  return 0;
+}
+
+#define MAK_QR_ENTRY(NAME, FULL, T, PT)                                                        \
+  int NAME(int64_t m, int64_t n, PT* A, int64_t lda, PT* Q, int64_t ldq, PT* R, int64_t ldr,   \
+           const mak_qr_opts* opts, void* work, size_t work_bytes, mak_info* info,             \
+           mak_stream_t stream) {                                                              \
+    return qr_entry<T>(FULL, m, n, A, lda, Q, ldq, R, ldr, opts, work, work_bytes, info,       \
+                       stream);                                                                \
+  }
+MAK_QR_ENTRY(mak_qr_compact_d, 0, double, double)
+MAK_QR_ENTRY(mak_qr_compact_z, 0, zcomplex, void)
+MAK_QR_ENTRY(mak_qr_compact_s, 0, float, float)
+MAK_QR_ENTRY(mak_qr_compact_c, 0, ccomplex, void)
+MAK_QR_ENTRY(mak_qr_full_d, 1, double, double)
+MAK_QR_ENTRY(mak_qr_full_z, 1, zcomplex, void)
+MAK_QR_ENTRY(mak_qr_full_s, 1, float, float)
+MAK_QR_ENTRY(mak_qr_full_c, 1, ccomplex, void)
+
+const char* mak_version(void) { return "mak_gb300 0.1.0 (sm_103a)"; }
+
+const char* mak_status_string(int code) {
+  if (code == MAK_OK) return "ok";
+  if (code < 0) return "invalid argument (-index of the offending argument)";
+  switch (code) {
+    case MAK_ERR_CUDA: return "CUDA launch or runtime error";
+    case MAK_ERR_TIMEOUT: return "bounded device-side wait gave up";
+    case MAK_ERR_UNSUPPORTED: return "shape outside the supported envelope";
+    case MAK_ERR_WORKSPACE: return "workspace too small";
+    default: return "unknown status";
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+"""CPU tests of the oracle (the checker), against known answers and the
+reference's own property tests (test/testsuite/decompositions/{qr,polar}.jl,
+test/testsuite/chainrules.jl)."""
+
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+DTYPES = [np.float64, np.complex128, np.float32, np.complex64]
+
+
+def prec(dt):
+    """``TestSuite.precision(T) = sqrt(eps(real(T)))`` (test/testsuite/TestSuite.jl:45)."""
+    return np.sqrt(O.eps(dt))
+
+
+@pytest.mark.parametrize("path", sorted(GOLD.glob("qr_kat_*.npz")), ids=lambda p: p.stem)
+def test_oracle_qr_known_answer(path):
+    d = np.load(path)
+    Q, R = O.qr_compact(d["A"])
+    assert O.rel_err(R, d["R"]) < 1e-12
+    assert O.rel_err(Q, d["Q"]) < 1e-12
+
+
+@pytest.mark.parametrize("path", sorted(GOLD.glob("polar_kat_*.npz")), ids=lambda p: p.stem)
+def test_oracle_polar_known_answer(path):
+    d = np.load(path)
+    for W, P in (O.left_polar_svd(d["A"]), O.left_polar_newton(d["A"])[:2]):
+        assert O.rel_err(W, d["W"]) < 1e-11
+        assert O.rel_err(P, d["P"]) < 1e-11
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("n", [37, 54, 63])
+def test_oracle_qr_properties(dt, n):
+    """test/testsuite/decompositions/qr.jl:22-113 at m = 54."""
+    rng = np.random.default_rng(123)
+    A = O.gaussian(rng, 54, n, dt)
+    for full in (False, True):
+        Q, R = (O.qr_full if full else O.qr_compact)(A)
+        assert O.qr_residual(A, Q, R) < prec(dt)
+        assert O.orth_error(Q) < prec(dt) * np.sqrt(Q.shape[1])
+        assert np.allclose(R, np.triu(R))
+        d = np.diagonal(R)
+        assert np.all(d.real >= 0) and np.all(np.abs(d.imag) == 0)
+    Qn, Rn = O.qr_compact(A, positive=False)
+    assert O.qr_residual(A, Qn, Rn) < prec(dt)
+    for bs in (1, 8):
+        Qb, Rb = O.qr_compact(A, blocksize=bs)
+        assert O.qr_residual(A, Qb, Rb) < prec(dt)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_polar_newton_vs_svd(dt):
+    rng = np.random.default_rng(5)
+    for (m, n) in ((54, 37), (54, 54), (120, 40)):
+        A = O.gaussian(rng, m, n, dt)
+        W1, P1 = O.left_polar_svd(A)
+        W2, P2, info = O.left_polar_newton(A)
+        assert info["converged"]
+        assert O.rel_err(W1, W2) < 1e-12 and O.rel_err(P1, P2) < 1e-12
+        assert O.orth_error(W2) < 1e-13 * n
+        assert np.linalg.norm(A - W2 @ P2) / np.linalg.norm(A) < 1e-13
+
+
+def test_oracle_newton_iteration_count_illconditioned():
+    rng = np.random.default_rng(2)
+    A = O.polar_test_matrix(rng, 128, np.float64)
+    W, P, info = O.left_polar_newton(A)
+    assert info["converged"] and 5 <= info["iterations"] <= 10
+    assert np.linalg.norm(A - W @ P) / np.linalg.norm(A) < 1e-12
+
+
+def test_oracle_sylvester_sign_convention():
+    """Julia sylvester(A,B,C) solves AX + XB + C = 0 (scipy: AX + XB = Q)."""
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((6, 6)) + 6 * np.eye(6)
+    B = rng.standard_normal((6, 6)) + 6 * np.eye(6)
+    Cm = rng.standard_normal((6, 6))
+    X = O.sylvester(A, B, Cm)
+    assert np.allclose(A @ X + X @ B + Cm, 0, atol=1e-12)
+
+
+def _fd(f, A, E, h=1e-6):
+    return (f(A + h * E) - f(A - h * E)) / (2 * h)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+@pytest.mark.parametrize("n", [17, 19, 23])
+def test_oracle_qr_pullback_fd(dt, n):
+    """Central finite differences, step 1e-6 (test/testsuite/chainrules.jl:53-145)."""
+    rng = np.random.default_rng(11)
+    m = 19
+    A = O.gaussian(rng, m, n, dt)
+    Q, R = O.qr_compact(A)
+    dQ, dR = O.gaussian(rng, *Q.shape, dt), O.gaussian(rng, *R.shape, dt)
+    dQ, dR = O.remove_qr_gauge_dependence(dQ, dR, A, Q, R)
+    dA, info = O.qr_pullback(np.zeros_like(A), A, Q, R, dQ, dR)
+    assert not info["warn"]
+    E = O.gaussian(rng, m, n, dt)
+
+    def loss(X):
+        Qx, Rx = O.qr_compact(X)
+        return np.real(np.vdot(dQ, Qx) + np.vdot(dR, Rx))
+
+    assert abs(_fd(loss, A, E) - np.real(np.vdot(dA, E))) < 1e-7 * max(1, abs(_fd(loss, A, E)))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_qr_pullback_rank_deficient_fd(dt):
+    """Rank-deficient A with a gauge-invariant cotangent
+    (test/testsuite/chainrules.jl:125-143)."""
+    rng = np.random.default_rng(12)
+    A = O.rank_deficient(rng, 30, 20, 14, dt)
+    Q, R = O.qr_compact(A)
+    dQ, dR = O.gaussian(rng, *Q.shape, dt), O.gaussian(rng, *R.shape, dt)
+    dQ, dR = O.remove_qr_gauge_dependence(dQ, dR, A, Q, R)
+    dA, info = O.qr_pullback(np.zeros_like(A), A, Q, R, dQ, dR)
+    assert info["rank"] == 14
+    # FD along directions that keep the rank (E = B1 C + B C1)
+    B = rng.standard_normal((30, 14)); Cm = rng.standard_normal((14, 20))
+    E = A @ np.linalg.pinv(A) @ O.gaussian(rng, 30, 20, dt) @ np.linalg.pinv(A) @ A
+
+    def loss(X):
+        Qx, Rx = O.qr_compact(X)
+        return np.real(np.vdot(dQ, Qx) + np.vdot(dR, Rx))
+
+    fd = _fd(loss, A, E)
+    assert abs(fd - np.real(np.vdot(dA, E))) < 1e-6 * max(1, abs(fd))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_polar_pullback_fd(dt):
+    rng = np.random.default_rng(13)
+    A = O.gaussian(rng, 19, 17, dt)
+    W, P = O.left_polar_svd(A)
+    dW, dP = O.gaussian(rng, 19, 17, dt), O.gaussian(rng, 17, 17, dt)
+    dA = O.left_polar_pullback(np.zeros_like(A), A, W, P, dW, dP)
+    E = O.gaussian(rng, 19, 17, dt)
+
+    def loss(X):
+        Wx, Px = O.left_polar_svd(X)
+        return np.real(np.vdot(dW, Wx) + np.vdot(dP, Px))
+
+    fd = _fd(loss, A, E)
+    assert abs(fd - np.real(np.vdot(dA, E))) < 1e-7 * max(1, abs(fd))
+
+
+def test_oracle_flop_counts():
+    assert abs(O.qr_flops(512, 256) - 0.1118e9) / 0.1118e9 < 1e-3
+    assert abs(O.qr_flops(16384, 8192) - 3.665e12) / 3.665e12 < 1e-3
