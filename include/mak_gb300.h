@@ -91,6 +91,19 @@ typedef struct {
 /* library identification */
 const char* mak_version(void);
 const char* mak_status_string(int code);
+/* number of CUDA kernels this library has launched in the process so far
+ * (profiling aid: a benchmark reads it before and after its timed region) */
+uint64_t mak_kernel_launches(void);
+
+/* Optional device-time accounting per kernel class: between start and stop,
+ * launches of the instrumented classes are bracketed by CUDA events on their
+ * stream; read waits for those events and returns the summed elapsed time,
+ * the summed algorithmic work (flops or bytes) and the launch count.
+ * kind: 0 native GEMM, 1 mixed-precision GEMM, 2 QR panel, 3 Gauss-Jordan
+ * panel, -1 all. */
+int mak_profile_start(void);
+int mak_profile_stop(void);
+int mak_profile_read(int kind, double* total_ms, double* total_work, uint64_t* launches);
 
 /* ------------------------------------------------------------------- QR ---
  * qr_compact!(A, (Q, R), GB300_HouseholderQR(; positive, blocksize))
@@ -126,6 +139,33 @@ int mak_qr_full_s(int64_t m, int64_t n, float* A, int64_t lda, float* Q, int64_t
 int mak_qr_full_c(int64_t m, int64_t n, void* A, int64_t lda, void* Q, int64_t ldq,
                   void* R, int64_t ldr, const mak_qr_opts* opts, void* work,
                   size_t work_bytes, mak_info* info, mak_stream_t stream);
+
+/* ---------------------------------------------------------------- polar ---
+ * left_polar!(A, (W, P), GB300_PolarNewton(; maxiter, tol))
+ * Replaces the reference's left_polar!(::PolarNewton) + left_polar_newton!
+ * (src/implementations/polar.jl:99-111,128-166), _avgdiff! (polar.jl:209-220)
+ * and project_hermitian! (src/implementations/projections.jl:61-108).
+ * m >= n required.  A (m x n) is destroyed.  W: m x n.  P: n x n Hermitian,
+ * or NULL (reference: empty P = not wanted, polar.jl:102-104).
+ * info->iterations / residual / converged report the Newton loop; a
+ * non-converged result is returned, not an error (the reference @warns,
+ * polar.jl:159-161).  The host synchronizes `stream` once per Newton
+ * iteration to evaluate the stopping test, like the reference's host loop.
+ */
+int mak_left_polar_workspace(int dtype, int64_t m, int64_t n, int want_p,
+                             const mak_polar_opts* opts, size_t* bytes);
+int mak_left_polar_newton_d(int64_t m, int64_t n, double* A, int64_t lda, double* W, int64_t ldw,
+                            double* P, int64_t ldp, const mak_polar_opts* opts, void* work,
+                            size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_left_polar_newton_z(int64_t m, int64_t n, void* A, int64_t lda, void* W, int64_t ldw,
+                            void* P, int64_t ldp, const mak_polar_opts* opts, void* work,
+                            size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_left_polar_newton_s(int64_t m, int64_t n, float* A, int64_t lda, float* W, int64_t ldw,
+                            float* P, int64_t ldp, const mak_polar_opts* opts, void* work,
+                            size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_left_polar_newton_c(int64_t m, int64_t n, void* A, int64_t lda, void* W, int64_t ldw,
+                            void* P, int64_t ldp, const mak_polar_opts* opts, void* work,
+                            size_t work_bytes, mak_info* info, mak_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -21,14 +21,15 @@ from . import _lib
 from .algorithms import (ArgumentError, DimensionMismatch, GB300_HouseholderQR,
                          GB300_PolarNewton, LeftOrthViaPolar, LeftOrthViaQR, default_algorithm,
                          is_positive, select_algorithm)
+from .polar import SingularException, left_polar, left_polar_
 from .qr import (initialize_output, qr_compact, qr_compact_, qr_full, qr_full_, qr_null,
                  qr_null_)
 
 __all__ = [
-    "ArgumentError", "DimensionMismatch", "GB300_HouseholderQR", "GB300_PolarNewton",
-    "LeftOrthViaQR", "LeftOrthViaPolar", "default_algorithm", "select_algorithm", "is_positive",
-    "qr_compact", "qr_compact_", "qr_full", "qr_full_", "qr_null", "qr_null_",
-    "initialize_output", "library",
+    "ArgumentError", "DimensionMismatch", "SingularException", "GB300_HouseholderQR",
+    "GB300_PolarNewton", "LeftOrthViaQR", "LeftOrthViaPolar", "default_algorithm",
+    "select_algorithm", "is_positive", "qr_compact", "qr_compact_", "qr_full", "qr_full_",
+    "qr_null", "qr_null_", "left_polar", "left_polar_", "initialize_output", "library",
 ]
 
 

@@ -47,6 +47,11 @@ _sz = C.c_size_t
 SIGNATURES = {
     "mak_version": (C.c_char_p, []),
     "mak_status_string": (C.c_char_p, [C.c_int]),
+    "mak_kernel_launches": (C.c_uint64, []),
+    "mak_profile_start": (C.c_int, []),
+    "mak_profile_stop": (C.c_int, []),
+    "mak_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_uint64)]),
     "mak_qr_workspace": (C.c_int, [C.c_int, _i64, _i64, C.c_int, C.POINTER(mak_qr_opts),
                                    C.POINTER(_sz)]),
 }
@@ -54,6 +59,12 @@ _QR_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, C.POINTER(mak_qr_opts), _p
 for _kind in ("compact", "full"):
     for _s in "dzsc":
         SIGNATURES[f"mak_qr_{_kind}_{_s}"] = (C.c_int, _QR_ARGS)
+SIGNATURES["mak_left_polar_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
+                                                    C.POINTER(mak_polar_opts), C.POINTER(_sz)])
+_POLAR_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, C.POINTER(mak_polar_opts), _p, _sz, _p,
+               _p]
+for _s in "dzsc":
+    SIGNATURES[f"mak_left_polar_newton_{_s}"] = (C.c_int, _POLAR_ARGS)
 
 _lib = None
 _load_error = None

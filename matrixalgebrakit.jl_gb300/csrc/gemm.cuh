@@ -144,6 +144,7 @@ int gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T> A
   if (M <= 0 || N <= 0) return 0;
   if (K <= 0) {
     dim3 g((unsigned)ceil_div(M, 256), (unsigned)N);
+    note_launch();
     scale_kernel<T><<<g, 256, 0, st>>>((int)M, (int)N, beta, C, ldc);
     return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
   }
@@ -153,12 +154,15 @@ int gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T> A
   splits = (int)ceil_div(K, kchunk);
   if (used_splits) *used_splits = splits;
   if (splits > 1) beta = zero_<T>();
+  ProfScope prof(st, PROF_GEMM_NATIVE, (traits<T>::cpx ? 8.0 : 2.0) * M * N * K);
   if (M <= 32) {
     dim3 g((unsigned)ceil_div(M, 32), (unsigned)ceil_div(N, 64), (unsigned)splits);
+    note_launch();
     gemm_kernel<T, 32, 64, BK, 2, 4><<<g, 256, 0, st>>>((int)M, (int)N, (int)K, alpha, A, B,
                                                          beta, C, ldc, kchunk, split_stride);
   } else {
     dim3 g((unsigned)ceil_div(M, 64), (unsigned)ceil_div(N, 64), (unsigned)splits);
+    note_launch();
     gemm_kernel<T, 64, 64, BK, 4, 4><<<g, 256, 0, st>>>((int)M, (int)N, (int)K, alpha, A, B,
                                                          beta, C, ldc, kchunk, split_stride);
   }

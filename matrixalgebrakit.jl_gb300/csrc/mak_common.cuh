@@ -9,6 +9,8 @@
 #include <stdint.h>
 #include <math.h>
 
+#include <atomic>
+
 #include "../../include/mak_gb300.h"
 
 namespace mak {
@@ -235,5 +237,27 @@ struct Arena {
 
 int num_sms();
 int max_smem_optin();
+
+// process-wide count of kernels this library has launched (mak_kernel_launches)
+std::atomic<unsigned long long>& launch_counter();
+inline void note_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
+
+// kernel classes timed by the optional profiler (mak_profile_*)
+enum ProfKind {
+  PROF_GEMM_NATIVE = 0,  // SIMT FP64/FP32 GEMM (work = flops)
+  PROF_GEMM_MIXED = 1,   // split-precision tensor-core GEMM (work = fp64-equivalent flops)
+  PROF_QR_PANEL = 2,     // cooperative Householder panel (work = bytes)
+  PROF_GJ_PANEL = 3      // cooperative Gauss-Jordan panel (work = bytes)
+};
+// RAII: records an event pair around the launches in its scope when the
+// profiler is on; a no-op otherwise.
+struct ProfScope {
+  cudaEvent_t e0 = nullptr;
+  cudaStream_t st;
+  int kind;
+  double work;
+  ProfScope(cudaStream_t s, int k, double w);
+  ~ProfScope();
+};
 
 }  // namespace mak

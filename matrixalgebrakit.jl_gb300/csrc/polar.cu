@@ -1,0 +1,501 @@
+// Left polar decomposition by the scaled Newton iteration, GB300 native.
+//
+// Replaces the reference's left_polar!(A, (W, P), ::PolarNewton)
+// (src/implementations/polar.jl:99-111) and left_polar_newton!
+// (polar.jl:128-166) with _avgdiff! (polar.jl:209-220; GPU kernel
+// ext/MatrixAlgebraKitCUDAExt/MatrixAlgebraKitCUDAExt.jl:154-173) and
+// project_hermitian! (src/implementations/projections.jl:61-108).
+//
+//   m > n : A = Q R (qr_run), iterate on X0 = R;   m == n : iterate on X0 = A
+//   X <- (g X + X^{-H}/g)/2,   g = sqrt(||X^{-H}||_F / ||X||_F)
+//   stop when max|X^{-H}/g - g X| <= tol  or after maxiter iterations
+//   W = Q X  (m > n)  or  W = X,     P = herm(W^H A)
+//
+// The inverse is an in-place blocked Gauss-Jordan elimination with partial
+// pivoting (gje_inverse): per block column of 32 a cooperative panel kernel
+// (pivot search + row exchange + elimination, two bounded grid barriers per
+// column, panel rows resident in shared memory), a row-exchange/save kernel
+// for the other columns and one rank-32 GEMM update -- 2n^3 flops in total,
+// the same count as the reference's LU + inverse.  The Newton update reads
+// X^{-H} straight out of the eliminated matrix through the inverse column
+// permutation (no separate transpose or permutation pass) and fuses the
+// avgdiff step, the scaling and the max-abs convergence measure.  For
+// m > n, P is formed as herm(X^H R) (= herm(W^H A) since A = QR, W = QX),
+// an n^3 instead of an m n^2 product.
+#include "gemm.cuh"
+#include "internal.h"
+#include "util.cuh"
+
+#include <climits>
+#include <mutex>
+
+namespace mak {
+
+constexpr int GJ_NB = 32;
+constexpr int GJ_THREADS = 256;
+
+template <class T>
+struct GjArgs {
+  T* X;
+  int64_t ldx;
+  int n, k0, b, rpc;
+  int* piv;
+  real_t<T>* part_val;
+  int* part_idx;
+  T* swapbuf;  // [2][GJ_NB]
+  unsigned* bar;
+  int* status;
+  int* singular;
+};
+
+__device__ __forceinline__ double cabs1_(double x) { return fabs(x); }
+__device__ __forceinline__ float cabs1_(float x) { return fabsf(x); }
+template <class R> __device__ __forceinline__ R cabs1_(cplx<R> x) { return fabs(x.re) + fabs(x.im); }
+
+// (value desc, index asc) arg-max merge
+template <class R>
+__device__ __forceinline__ void amax_merge(R& v, int& i, R v2, int i2) {
+  if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
+}
+
+template <class T>
+__global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
+  using R = real_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x b, ld = rpc
+  __shared__ R sv[32];
+  __shared__ int si[32];
+  __shared__ T prow[GJ_NB];
+  __shared__ int pivs;
+  const int G = gridDim.x, cb = blockIdx.x, tid = threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  const int rpc = a.rpc, b = a.b, k0 = a.k0;
+  const int r0 = cb * rpc;
+  const int nr = max(0, min(a.n, r0 + rpc) - r0);
+  T* Xp = a.X + (int64_t)k0 * a.ldx;
+  for (int c = 0; c < b; c++)
+    for (int r = tid; r < nr; r += blockDim.x) Ps[r + c * rpc] = Xp[(r0 + r) + (int64_t)c * a.ldx];
+  __syncthreads();
+
+  for (int j = 0; j < b; j++) {
+    const int jj = k0 + j;
+    // ---- pivot search over global rows >= jj
+    R best = R(-1);
+    int bidx = INT_MAX;
+    for (int r = tid; r < nr; r += blockDim.x) {
+      const int gr = r0 + r;
+      if (gr >= jj) amax_merge(best, bidx, cabs1_(Ps[r + j * rpc]), gr);
+    }
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) {
+      R v2 = __shfl_xor_sync(0xffffffffu, best, m);
+      int i2 = __shfl_xor_sync(0xffffffffu, bidx, m);
+      amax_merge(best, bidx, v2, i2);
+    }
+    if (lane == 0) { sv[wid] = best; si[wid] = bidx; }
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < nw; w++) amax_merge(best, bidx, sv[w], si[w]);
+      a.part_val[cb] = best;
+      a.part_idx[cb] = bidx;
+    }
+    if (!grid_barrier(a.bar, G, a.status)) return;
+
+    // ---- global pivot (identical in every CTA), publish the two rows
+    if (wid == 0) {
+      R v = R(-1);
+      int ix = INT_MAX;
+      for (int q = lane; q < G; q += 32) amax_merge(v, ix, ld_cg(&a.part_val[q]), ld_cg(&a.part_idx[q]));
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1) {
+        R v2 = __shfl_xor_sync(0xffffffffu, v, m);
+        int i2 = __shfl_xor_sync(0xffffffffu, ix, m);
+        amax_merge(v, ix, v2, i2);
+      }
+      if (lane == 0) pivs = (ix == INT_MAX) ? jj : ix;
+    }
+    __syncthreads();
+    const int p = pivs;
+    if (jj >= r0 && jj < r0 + nr)
+      for (int c = tid; c < b; c += blockDim.x) a.swapbuf[c] = Ps[(jj - r0) + c * rpc];
+    if (p >= r0 && p < r0 + nr)
+      for (int c = tid; c < b; c += blockDim.x) a.swapbuf[GJ_NB + c] = Ps[(p - r0) + c * rpc];
+    if (cb == 0 && tid == 0) a.piv[jj] = p;
+    if (!grid_barrier(a.bar, G, a.status)) return;
+
+    // ---- exchange rows jj <-> p, then eliminate column jj from every other row
+    for (int c = tid; c < b; c += blockDim.x) prow[c] = ld_cg(&a.swapbuf[GJ_NB + c]);
+    if (p != jj && p >= r0 && p < r0 + nr)
+      for (int c = tid; c < b; c += blockDim.x) Ps[(p - r0) + c * rpc] = ld_cg(&a.swapbuf[c]);
+    __syncthreads();
+    const T d = prow[j];
+    if (d == zero_<T>()) {
+      if (tid == 0) atomicExch(a.singular, 1);
+    }
+    const T dinv = inv_(d);
+    for (int r = tid; r < nr; r += blockDim.x) {
+      const int gr = r0 + r;
+      if (gr == jj) {
+        for (int c = 0; c < b; c++) Ps[r + c * rpc] = (c == j) ? dinv : prow[c] * dinv;
+      } else {
+        const T f = Ps[r + j * rpc];
+        for (int c = 0; c < b; c++) {
+          if (c == j) Ps[r + c * rpc] = -(f * dinv);
+          else Ps[r + c * rpc] -= f * (prow[c] * dinv);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int c = 0; c < b; c++)
+    for (int r = tid; r < nr; r += blockDim.x) Xp[(r0 + r) + (int64_t)c * a.ldx] = Ps[r + c * rpc];
+}
+
+// For every column outside the panel: apply the panel's row exchanges in
+// order, save rows k0..k0+b-1 into buf (b x n) and zero them in X.
+template <class T>
+__global__ void gje_laswp_save_kernel(int n, T* X, int64_t ldx, int k0, int b, const int* piv,
+                                      T* buf) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n || (c >= k0 && c < k0 + b)) return;
+  T* col = X + (int64_t)c * ldx;
+  for (int t = 0; t < b; t++) {
+    const int jj = k0 + t, p = piv[jj];
+    if (p != jj && p >= 0 && p < n) {
+      T x = col[jj];
+      col[jj] = col[p];
+      col[p] = x;
+    }
+  }
+  for (int t = 0; t < b; t++) {
+    buf[t + (int64_t)c * b] = col[k0 + t];
+    col[k0 + t] = zero_<T>();
+  }
+}
+
+__global__ void iota_kernel(int n, int* v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+
+// iperm = inverse of the composed row permutation
+__global__ void gje_perm_kernel(int n, const int* piv, int* iperm) {
+  extern __shared__ int perm[];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int jj = 0; jj < n; jj++) {
+      const int p = piv[jj];
+      if (p != jj && p >= 0 && p < n) {
+        int t = perm[jj];
+        perm[jj] = perm[p];
+        perm[p] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) iperm[perm[i]] = i;
+}
+
+template <class T>
+static size_t gj_slab_cap() {
+  static size_t cap = 0;
+  static std::once_flag f;
+  std::call_once(f, [] {
+    cudaFuncAttributes fa;
+    size_t stat = 16 * 1024;
+    if (cudaFuncGetAttributes(&fa, gje_panel_kernel<T>) == cudaSuccess) stat = fa.sharedSizeBytes;
+    cap = (size_t)max_smem_optin() - stat - 1024;
+    cudaFuncSetAttribute(gje_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)cap);
+    cudaFuncSetAttribute(gje_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         max_smem_optin() - 1024);
+  });
+  return cap;
+}
+
+template <class T>
+int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int precision,
+                Arena& ar, mak_info* info) {
+  (void)precision;
+  const int sms = num_sms();
+  int* piv = ar.take<int>(n > 0 ? n : 1);
+  real_t<T>* part_val = ar.take<real_t<T>>(sms);
+  int* part_idx = ar.take<int>(sms);
+  T* swapbuf = ar.take<T>(2 * GJ_NB);
+  T* buf = ar.take<T>((size_t)GJ_NB * (n > 0 ? n : 1));
+  unsigned* bar = ar.take<unsigned>(2);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  if (n <= 0) return 0;
+  if ((size_t)n * sizeof(int) > (size_t)max_smem_optin() - 1024) return MAK_ERR_UNSUPPORTED;
+  MAK_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
+  // pivots start as the identity so that an aborted panel (bounded barrier
+  // timeout) still leaves every index in range
+  note_launch();
+  iota_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>((int)n, piv);
+  const size_t cap = gj_slab_cap<T>();
+  for (int64_t k0 = 0; k0 < n; k0 += GJ_NB) {
+    const int b = (int)((n - k0) < GJ_NB ? (n - k0) : GJ_NB);
+    // grid: rows per CTA >= 64, one CTA per SM, slab within shared memory
+    int64_t G = ceil_div(n, 64);
+    if (G > sms) G = sms;
+    int64_t rpc = ceil_div(n, G);
+    if ((size_t)rpc * b * sizeof(T) > cap) return MAK_ERR_UNSUPPORTED;
+    G = ceil_div(n, rpc);
+    size_t smem = (size_t)rpc * b * sizeof(T);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_kernel<T>, GJ_THREADS,
+                                                      smem) != cudaSuccess ||
+        (int64_t)per_sm * sms < G)
+      return MAK_ERR_UNSUPPORTED;
+    GjArgs<T> ga{X, ldx, (int)n, (int)k0, b, (int)rpc, piv, part_val, part_idx, swapbuf,
+                 bar, &info->status, &info->singular};
+    void* args[] = {&ga};
+    ProfScope prof(st, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
+    note_launch();
+    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)gje_panel_kernel<T>, dim3((unsigned)G),
+                                             dim3(GJ_THREADS), args, smem, st));
+    note_launch();
+    gje_laswp_save_kernel<T><<<(unsigned)ceil_div(n, 128), 128, 0, st>>>((int)n, X, ldx, (int)k0,
+                                                                         b, piv, buf);
+    MAK_CUDA_TRY(cudaGetLastError());
+    const T* F = X + k0 * ldx;
+    if (k0 > 0)
+      MAK_TRY(gemm<T>(st, n, k0, b, one_<T>(), opnd<T>(F, ldx), opnd<T>(buf, b), one_<T>(), X,
+                      ldx));
+    if (k0 + b < n)
+      MAK_TRY(gemm<T>(st, n, n - k0 - b, b, one_<T>(), opnd<T>(F, ldx),
+                      opnd<T>(buf + (k0 + b) * b, b), one_<T>(), X + (k0 + b) * ldx, ldx));
+  }
+  note_launch();
+  gje_perm_kernel<<<1, 1024, (size_t)n * sizeof(int), st>>>((int)n, piv, iperm);
+  MAK_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// ---- Newton step -----------------------------------------------------------
+__device__ __forceinline__ void atomic_max_nonneg(double* addr, double v) {
+  atomicMax((unsigned long long*)addr, (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void atomic_max_nonneg(float* addr, float v) {
+  atomicMax((unsigned int*)addr, __float_as_uint(v));
+}
+
+// X <- (g X + Y^H/g)/2 with Y^H[i,j] = conj(Xi[j, iperm[i]]) (Xi = eliminated
+// inverse), g = (||Xi||_F^2 / ||X||_F^2)^(1/4); *conv = max |Y^H/g - g X|.
+template <class T>
+__global__ void __launch_bounds__(256) newton_update_kernel(int n, T* X, int64_t ldx,
+                                                            const T* Xi, int64_t ldi,
+                                                            const int* iperm,
+                                                            const real_t<T>* nrm2,
+                                                            real_t<T>* conv) {
+  using R = real_t<T>;
+  __shared__ T t[32][33];
+  __shared__ R sh[32];
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + r, j = j0 + tx;
+    t[r][tx] = (i < n && j < n) ? Xi[j + (int64_t)iperm[i] * ldi] : zero_<T>();  // t[i'][j'] = Xi[j, iperm[i]]
+  }
+  __syncthreads();
+  const R g = sqrt(sqrt(nrm2[1] / nrm2[0]));
+  const R ginv = R(1) / g;
+  R dmax = R(0);
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, j = j0 + r;
+    if (i < n && j < n) {
+      const T y = conj_(t[tx][r]) * ginv;
+      const T x = g * X[i + (int64_t)j * ldx];
+      X[i + (int64_t)j * ldx] = R(0.5) * (x + y);
+      dmax = fmax(dmax, abs_(y - x));
+    }
+  }
+  dmax = block_max(dmax, sh);
+  if (threadIdx.x == 0) atomic_max_nonneg(conv, dmax);
+}
+
+template <class T>
+__global__ void info_polar_kernel(mak_info* info, int it, double conv, int converged) {
+  info->iterations = it;
+  info->residual = conv;
+  info->converged = converged;
+}
+
+template <class T>
+int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* W, int64_t ldw,
+                     T* P, int64_t ldp, int maxiter, double tol, int precision, Arena& ar,
+                     mak_info* info) {
+  using R = real_t<T>;
+  const bool want_p = P != nullptr;
+  T* X = ar.take<T>((size_t)n * n + 1);
+  T* Y = ar.take<T>((size_t)n * n + 1);
+  int* iperm = ar.take<int>(n + 1);
+  R* red = ar.take<R>(RED_CTAS + 8);
+  T* Qw = (m > n) ? ar.take<T>((size_t)m * n) : nullptr;
+  T* Rw = (m > n) ? ar.take<T>((size_t)n * n) : nullptr;
+  T* A0 = (m == n && want_p) ? ar.take<T>((size_t)n * n) : nullptr;
+  // the QR (m > n, once) and Gauss-Jordan (every iteration) workspaces are
+  // used one after the other, so they share one tail region
+  size_t qr_ws = 0, gj_ws = 0;
+  if (m > n) {
+    Arena meas(nullptr, 0);
+    qr_run<T>(st, m, n, nullptr, lda, nullptr, m, n, nullptr, n, n, 1, 0, precision, meas,
+              nullptr);
+    qr_ws = meas.off + 256;
+  }
+  {
+    Arena meas(nullptr, 0);
+    gje_inverse<T>(st, n, nullptr, n, nullptr, precision, meas, nullptr);
+    gj_ws = meas.off + 256;
+  }
+  const size_t tail_bytes = qr_ws > gj_ws ? qr_ws : gj_ws;
+  char* tail = ar.take<char>(tail_bytes);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  R* nrm2 = red + RED_CTAS;      // [0] ||X||^2, [1] ||Xi||^2
+  R* conv = red + RED_CTAS + 2;  // max |D|
+
+  if (m > n) {
+    Arena sub(tail, tail_bytes);
+    MAK_TRY(qr_run<T>(st, m, n, A, lda, Qw, m, n, Rw, n, n, 1, 0, precision, sub, info));
+    MAK_TRY(copy_mat<T>(st, n, n, Rw, n, X, n));
+  } else {
+    if (want_p) MAK_TRY(copy_mat<T>(st, n, n, A, lda, A0, n));
+    MAK_TRY(copy_mat<T>(st, n, n, A, lda, X, n));
+  }
+  int it = 0;
+  R hconv = R(0);
+  bool converged = (n == 0);
+  for (it = 1; it <= maxiter && n > 0; it++) {
+    MAK_TRY(copy_mat<T>(st, n, n, X, n, Y, n));
+    {
+      Arena sub(tail, tail_bytes);
+      MAK_TRY(gje_inverse<T>(st, n, Y, n, iperm, precision, sub, info));
+    }
+    MAK_TRY(reduce_mat<T>(st, n, n, X, n, 0, red, nrm2));
+    MAK_TRY(reduce_mat<T>(st, n, n, Y, n, 0, red, nrm2 + 1));
+    MAK_CUDA_TRY(cudaMemsetAsync(conv, 0, sizeof(R), st));
+    dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+    note_launch();
+    newton_update_kernel<T><<<g, 256, 0, st>>>((int)n, X, n, Y, n, iperm, nrm2, conv);
+    MAK_CUDA_TRY(cudaGetLastError());
+    MAK_CUDA_TRY(cudaMemcpyAsync(&hconv, conv, sizeof(R), cudaMemcpyDeviceToHost, st));
+    MAK_CUDA_TRY(cudaStreamSynchronize(st));
+    if (!(hconv > (R)tol)) {  // also stops on NaN
+      converged = hconv <= (R)tol;
+      break;
+    }
+  }
+  if (it > maxiter) it = maxiter;
+  note_launch();
+  info_polar_kernel<T><<<1, 1, 0, st>>>(info, n > 0 ? it : 0, (double)hconv, converged ? 1 : 0);
+  MAK_CUDA_TRY(cudaGetLastError());
+
+  if (m > n) {
+    MAK_TRY(gemm<T>(st, m, n, n, one_<T>(), opnd<T>(Qw, m), opnd<T>(X, n), zero_<T>(), W, ldw));
+    if (want_p) {
+      MAK_TRY(gemm<T>(st, n, n, n, one_<T>(), opnd<T>(X, n, OP_C), opnd<T>(Rw, n, OP_N, MASK_UPPER),
+                      zero_<T>(), P, ldp));
+      MAK_TRY(herm_project<T>(st, n, P, ldp));
+    }
+  } else {
+    MAK_TRY(copy_mat<T>(st, n, n, X, n, W, ldw));
+    if (want_p) {
+      MAK_TRY(gemm<T>(st, n, n, n, one_<T>(), opnd<T>(X, n, OP_C), opnd<T>(A0, n), zero_<T>(), P,
+                      ldp));
+      MAK_TRY(herm_project<T>(st, n, P, ldp));
+    }
+  }
+  return 0;
+}
+
+#define MAK_INST_POLAR(T)                                                                     \
+  template int gje_inverse<T>(cudaStream_t, int64_t, T*, int64_t, int*, int, Arena&,          \
+                              mak_info*);                                                     \
+  template int polar_newton_run<T>(cudaStream_t, int64_t, int64_t, T*, int64_t, T*, int64_t, \
+                                   T*, int64_t, int, double, int, Arena&, mak_info*);
+MAK_INST_POLAR(double)
+MAK_INST_POLAR(float)
+MAK_INST_POLAR(zcomplex)
+MAK_INST_POLAR(ccomplex)
+
+template <class T>
+static double default_tol() {
+  // defaulttol = eps(real T)^(2/3)  (src/common/defaults.jl:10)
+  return pow(sizeof(real_t<T>) == 8 ? 2.220446049250313e-16 : 1.1920928955078125e-7, 2.0 / 3.0);
+}
+
+template <class T>
+static int polar_entry(int64_t m, int64_t n, void* Av, int64_t lda, void* Wv, int64_t ldw,
+                       void* Pv, int64_t ldp, const mak_polar_opts* opts, void* work,
+                       size_t work_bytes, mak_info* info, mak_stream_t stream) {
+  T* A = (T*)Av;
+  T* W = (T*)Wv;
+  T* P = (T*)Pv;
+  if (m < 0) return -1;
+  if (n < 0 || n > m) return -2;  // m >= n required (polar.jl:9-10)
+  if (A == nullptr && m * n > 0) return -3;
+  if (lda < (m > 1 ? m : 1)) return -4;
+  if (W == nullptr && m * n > 0) return -5;
+  if ((void*)W == (void*)A && m * n > 0) return -5;
+  if (ldw < (m > 1 ? m : 1)) return -6;
+  if (P != nullptr && ldp < (n > 1 ? n : 1)) return -8;
+  mak_polar_opts o{10, MAK_PREC_NATIVE, 0.0};
+  if (opts) o = *opts;
+  if (o.maxiter < 1) return -9;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -9;
+  const double tol = o.tol > 0 ? o.tol : default_tol<T>();
+  if (info == nullptr) return -12;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    polar_newton_run<T>(st, m, n, nullptr, lda, nullptr, ldw, P, ldp, o.maxiter, tol, o.precision,
+                        meas, nullptr);
+    if (meas.off > work_bytes) return -11;
+  }
+  Arena ar(work, work_bytes);
+  MAK_TRY(info_reset(st, info));
+  return polar_newton_run<T>(st, m, n, A, lda, W, ldw, P, ldp, o.maxiter, tol, o.precision, ar,
+                             info);
+}
+
+}  // namespace mak
+
+using namespace mak;
+
+extern "C" {
+
+int mak_left_polar_workspace(int dtype, int64_t m, int64_t n, int want_p,
+                             const mak_polar_opts* opts, size_t* bytes) {
+  if (bytes == nullptr) return -6;
+  if (m < 0) return -2;
+  if (n < 0 || n > m) return -3;
+  mak_polar_opts o{10, MAK_PREC_NATIVE, 0.0};
+  if (opts) o = *opts;
+  Arena meas(nullptr, 0);
+  void* P = want_p ? (void*)16 : nullptr;  // only nullness matters when measuring
+  switch (dtype) {
+    case MAK_F64: polar_newton_run<double>(0, m, n, nullptr, m, nullptr, m, (double*)P, n, o.maxiter, 1.0, o.precision, meas, nullptr); break;
+    case MAK_C64: polar_newton_run<zcomplex>(0, m, n, nullptr, m, nullptr, m, (zcomplex*)P, n, o.maxiter, 1.0, o.precision, meas, nullptr); break;
+    case MAK_F32: polar_newton_run<float>(0, m, n, nullptr, m, nullptr, m, (float*)P, n, o.maxiter, 1.0, o.precision, meas, nullptr); break;
+    case MAK_C32: polar_newton_run<ccomplex>(0, m, n, nullptr, m, nullptr, m, (ccomplex*)P, n, o.maxiter, 1.0, o.precision, meas, nullptr); break;
+    default: return -1;
+  }
+  *bytes = meas.off + 256;
+  return 0;
+}
+
+#define MAK_POLAR_ENTRY(NAME, T, PT)                                                            \
+  int NAME(int64_t m, int64_t n, PT* A, int64_t lda, PT* W, int64_t ldw, PT* P, int64_t ldp,    \
+           const mak_polar_opts* opts, void* work, size_t work_bytes, mak_info* info,           \
+           mak_stream_t stream) {                                                               \
+    return polar_entry<T>(m, n, A, lda, W, ldw, P, ldp, opts, work, work_bytes, info, stream); \
+  }
+MAK_POLAR_ENTRY(mak_left_polar_newton_d, double, double)
+MAK_POLAR_ENTRY(mak_left_polar_newton_z, zcomplex, void)
+MAK_POLAR_ENTRY(mak_left_polar_newton_s, float, float)
+MAK_POLAR_ENTRY(mak_left_polar_newton_c, ccomplex, void)
+
+}  // extern "C"

@@ -306,8 +306,14 @@ __global__ void info_reset_kernel(mak_info* info) {
 }
 
 int info_reset(cudaStream_t st, mak_info* info) {
+  note_launch();
   info_reset_kernel<<<1, 1, 0, st>>>(info);
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+}
+
+std::atomic<unsigned long long>& launch_counter() {
+  static std::atomic<unsigned long long> c{0};
+  return c;
 }
 
 int num_sms() {
@@ -425,6 +431,8 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     PanelArgs<T> pa{Ap, lda, (int)mp, jb, ps.rpc, tau + j0, Tb, part_nrm, part_w,
                     part_g, alpha_buf, bar, status};
     void* args[] = {&pa};
+    ProfScope prof(st, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
+    note_launch();
     MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)qr_panel_kernel<T>, dim3(ps.G),
                                              dim3(PANEL_THREADS), args, ps.smem, st));
     const int64_t nt = n - j0 - jb;
@@ -435,6 +443,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
       int used = 1;
       MAK_TRY(gemm<T>(st, jb, nt, mp, one_<T>(), opnd<T>(Ap, lda, OP_C, MASK_UNIT_LOWER),
                       opnd<T>(C, lda), zero_<T>(), Wpart, jb, splits, (int64_t)jb * nt, &used));
+      note_launch();
       reduce_trmm_kernel<T><<<(unsigned)ceil_div(nt, 32), 256, 0, st>>>(
           jb, (int)nt, used, Wpart, (int64_t)jb * nt, Tb, 1, W2);
       MAK_CUDA_TRY(cudaGetLastError());
@@ -445,16 +454,19 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
 
   // ------------------------------------------------------ R and the gauge
   if (k > 0) {
+    note_launch();
     signs_kernel<T><<<(unsigned)ceil_div(k, 256), 256, 0, st>>>((int)k, A, lda, positive, sgn);
     MAK_CUDA_TRY(cudaGetLastError());
   }
   if (R != nullptr && rrows > 0 && n > 0) {
     dim3 g((unsigned)ceil_div(rrows, 256), (unsigned)(n < 65535 ? n : 65535));
+    note_launch();
     extract_r_kernel<T><<<g, 256, 0, st>>>(rrows, n, k, A, lda, sgn, R, ldr);
     MAK_CUDA_TRY(cudaGetLastError());
   }
   if (m > 0 && qcols > 0) {
     dim3 g((unsigned)ceil_div(m, 256), (unsigned)(qcols < 65535 ? qcols : 65535));
+    note_launch();
     init_q_kernel<T><<<g, 256, 0, st>>>(m, qcols, k, sgn, Q, ldq);
     MAK_CUDA_TRY(cudaGetLastError());
   }
@@ -474,6 +486,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     int used = 1;
     MAK_TRY(gemm<T>(st, jb, qt, mp, one_<T>(), opnd<T>(Ap, lda, OP_C, MASK_UNIT_LOWER),
                     opnd<T>(Qs, ldq), zero_<T>(), Wpart, jb, splits, (int64_t)jb * qt, &used));
+    note_launch();
     reduce_trmm_kernel<T><<<(unsigned)ceil_div(qt, 32), 256, 0, st>>>(
         jb, (int)qt, used, Wpart, (int64_t)jb * qt, Tb, 0, W2);
     MAK_CUDA_TRY(cudaGetLastError());
@@ -576,6 +589,8 @@ MAK_QR_ENTRY(mak_qr_full_d, 1, double, double)
 MAK_QR_ENTRY(mak_qr_full_z, 1, zcomplex, void)
 MAK_QR_ENTRY(mak_qr_full_s, 1, float, float)
 MAK_QR_ENTRY(mak_qr_full_c, 1, ccomplex, void)
+
+uint64_t mak_kernel_launches(void) { return (uint64_t)launch_counter().load(); }
 
 const char* mak_version(void) { return "mak_gb300 0.1.0 (sm_103a)"; }
 

@@ -21,6 +21,7 @@ inline int copy_mat(cudaStream_t st, int64_t m, int64_t n, const T* A, int64_t l
                     int64_t ldb) {
   if (m <= 0 || n <= 0) return 0;
   dim3 g((unsigned)ceil_div(m, 256), (unsigned)(n < 65535 ? n : 65535));
+  note_launch();
   copy_kernel<T><<<g, 256, 0, st>>>(m, n, A, lda, B, ldb);
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
@@ -35,6 +36,7 @@ template <class T>
 inline int set_identity(cudaStream_t st, int64_t m, int64_t n, T* B, int64_t ldb) {
   if (m <= 0 || n <= 0) return 0;
   dim3 g((unsigned)ceil_div(m, 256), (unsigned)(n < 65535 ? n : 65535));
+  note_launch();
   set_identity_kernel<T><<<g, 256, 0, st>>>(m, n, B, ldb);
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
@@ -79,8 +81,10 @@ inline int reduce_mat(cudaStream_t st, int64_t m, int64_t n, const T* A, int64_t
   int64_t total = m * n;
   int g = (int)(total <= 0 ? 1 : ceil_div(total, 256));
   if (g > RED_CTAS) g = RED_CTAS;
+  note_launch();
   reduce_partial_kernel<T><<<g, 256, 0, st>>>(m > 0 ? m : 1, total > 0 ? n : 0, A, lda, kind,
                                               part);
+  note_launch();
   reduce_final_kernel<real_t<T>><<<1, 256, 0, st>>>(g, part, kind, out);
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
@@ -123,6 +127,7 @@ template <class T>
 inline int herm_project(cudaStream_t st, int64_t n, T* A, int64_t lda) {
   if (n <= 0) return 0;
   dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+  note_launch();
   herm_project_kernel<T><<<g, 256, 0, st>>>(n, A, lda);
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
