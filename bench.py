@@ -1,0 +1,496 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 orthogonal-factorization hot path.
+
+Default workload (the single large Float64 problem the headline metric is
+quoted on): ``qr_compact!(A, (Q, R); positive=true)`` of one 16384 x 8192
+Float64 matrix with iid N(0,1) entries (seeded numpy generator; synthetic --
+the reference names no dataset).  A step = restore A from a device-resident
+master copy (the factorization destroys its input) + the factorization.
+The matrix (1.07 GB) is larger than L2 (129 MB), so no flush is needed.
+
+Printed (rank 0, one JSON line): QR TFLOP/s with the minimal
+geqrf + orgqr flop count 4mn^2 - 4n^3/3 (``value``), the same through the
+public API with host buffers (``e2e``), factorizations/s, accuracy of every
+result (||A-QR||/||A||, ||Q^H Q - I||), the dominant kernel's roofline
+(device time measured live with CUDA events inside the timed region),
+SM clocks sampled during the timed region, the CPU baseline (the
+reference's LAPACK_HouseholderQR path restated with scipy/OpenBLAS on the
+host cores) and a left_polar! (Newton) measurement on an 8192 x 8192
+kappa = 1e6 matrix.
+
+``--impl reference`` times the reference's CPU implementation of the same
+path (the oracle restatement of LAPACK_HouseholderQR: ?geqrt + ?gemqrt +
+gaugefix, all host threads) and prints the same JSON line with
+``"impl": "reference"``.
+
+Multi-GPU: single matrices do not shard (a reduction tree would be needed),
+so N GPUs run N independent replicas ("scaling": "weak"); value = total
+flops of all ranks / max-over-ranks time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = ("QR/polar TFLOP/s + batched solves/s, mixed vs FP64 at "
+          "‖A−QR‖/‖A‖≤1e-12")
+SEED = 20260101
+OZ_PAIRS = 45  # bf16 plane products per FP64 product in the split GEMM (9 slices)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--precision", choices=["native", "mixed"], default="native")
+    ap.add_argument("--m", type=int, default=16384)
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--cpu-sample", type=str, default="8192x4096",
+                    help="bounded CPU-baseline sample (m x n of the same distribution)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lean", action="store_true",
+                    help="timed region only (profiling runs): no accuracy check, peak, e2e, "
+                         "polar or CPU baseline")
+    ap.add_argument("--no-polar", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--polar-n", type=int, default=8192)
+    return ap.parse_args()
+
+
+def qr_flops(m, n, cpx=False):
+    k = min(m, n)
+    geqrf = 2.0 * m * n * n - 2.0 * n ** 3 / 3.0 if m >= n else 2.0 * n * m * m - 2.0 * m ** 3 / 3.0
+    orgqr = 2.0 * m * k * k - 2.0 * k ** 3 / 3.0
+    return (4.0 if cpx else 1.0) * (geqrf + orgqr)
+
+
+def polar_flops(m, n, k_ref, cpx=False):
+    c = 4.0 if cpx else 1.0
+    f = (qr_flops(m, n, cpx) + c * 2.0 * m * n * n) if m > n else 0.0
+    return f + c * k_ref * 8.0 * n ** 3 / 3.0 + c * 2.0 * m * n * n
+
+
+def world():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+# ------------------------------------------------------------- clocks ---
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons (200 ms)."""
+
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str):
+        self.uuid = uuid.replace("GPU-", "")
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 8 or self.uuid not in parts[0].replace("GPU-", ""):
+                    continue
+                rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return float("nan")
+
+        sm = [num(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(num(r[2]) for r in rows),
+                "power_w_max": max(num(r[3]) for r in rows), "samples": len(rows),
+                "reasons": reasons}
+
+
+# -------------------------------------------------------- CPU baseline ---
+class _blas_threads:
+    """All host cores for OpenBLAS: threadpoolctl when installed, otherwise
+    OpenBLAS's own default (one thread per available core)."""
+
+    def __init__(self, cores):
+        self.cores = cores
+        self.ctx = None
+
+    def __enter__(self):
+        try:
+            import threadpoolctl
+
+            self.ctx = threadpoolctl.threadpool_limits(self.cores)
+            self.ctx.__enter__()
+        except ImportError:
+            self.ctx = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.ctx is not None:
+            self.ctx.__exit__(*exc)
+
+    @staticmethod
+    def describe():
+        try:
+            import threadpoolctl
+
+            return ",".join(f"{d.get('internal_api')} {d.get('version')} "
+                            f"threads={d.get('num_threads')}"
+                            for d in threadpoolctl.threadpool_info())
+        except ImportError:
+            return "scipy-bundled OpenBLAS (threadpoolctl absent: default thread count)"
+
+
+def cpu_qr_rate(m, n, reps=1):
+    """The reference's LAPACK_HouseholderQR path (oracle restatement) on all
+    host cores; returns (TFLOP/s, seconds per factorization, threads)."""
+    import numpy as np
+
+    import oracle
+
+    cores = len(os.sched_getaffinity(0))
+    rng = np.random.default_rng(SEED + 1)
+    A = oracle.gaussian(rng, m, n, np.float64)
+    with _blas_threads(cores):
+        oracle.qr_compact(A[: min(m, 512), : min(n, 256)])  # warm the BLAS threads
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            oracle.qr_compact(A)
+            ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    return qr_flops(m, n) / t / 1e12, t, cores
+
+
+def run_reference(args):
+    rank, ws, _ = world()
+    if rank != 0:
+        return 0
+    ms, ns = (int(x) for x in args.cpu_sample.split("x"))
+    import numpy as np
+
+    import oracle
+
+    cores = len(os.sched_getaffinity(0))
+    rng = np.random.default_rng(SEED)
+    A = oracle.gaussian(rng, ms, ns, np.float64)
+    with _blas_threads(cores):
+        for _ in range(args.warmup):
+            oracle.qr_compact(A)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            Q, R = oracle.qr_compact(A)
+        dt = (time.perf_counter() - t0) / args.steps
+        blas = _blas_threads.describe()
+    val = qr_flops(ms, ns) / dt / 1e12
+    sample = (f"qr_compact positive=true {ms}x{ns} Float64 per step (bounded sample of the "
+              f"{args.m}x{args.n} workload, same distribution)")
+    out = {
+        "impl": "reference", "metric": METRIC, "value": round(val, 5), "unit": "TFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic iid N(0,1), seeded",
+        "config": config_of(args),
+        "cpu_baseline": {"value": round(val, 5), "unit": "TFLOP/s", "cores": cores,
+                         "kind": "port", "sample": sample, "blas": blas},
+        "e2e": {"value": round(val, 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "accuracy": {"qr_residual": oracle.qr_residual(A, Q, R)},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def config_of(args):
+    return {"workload": f"qr_compact! positive=true, one {args.m}x{args.n} Float64 matrix, "
+                        f"iid N(0,1)", "m": args.m, "n": args.n, "precision": args.precision,
+            "parallelism": f"replicas x{args.gpus}",
+            "l2": "inputs larger than L2 (A is %.2f GB > 129 MB L2), no flush needed"
+                  % (args.m * args.n * 8 / 1e9)}
+
+
+# ------------------------------------------------------------ GB300 arm ---
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+
+    rank, ws, lrank = world()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = dist_mod
+    dev = torch.device(f"cuda:{lrank}")
+    torch.cuda.set_device(dev)
+    mak = ge.load_package()
+    lib = mak.library()
+    m, n = args.m, args.n
+    alg = mak.GB300_HouseholderQR(positive=True, precision=args.precision)
+
+    rng = np.random.default_rng(SEED + rank)
+    A_host = torch.from_numpy(rng.standard_normal((n, m))).t()  # column-major view
+    A_master = torch.empty((n, m), dtype=torch.float64, device=dev).t()
+    A_master.copy_(A_host)
+    A = torch.empty_like(A_master)
+    Q, R = mak.initialize_output("qr_compact_", A_master)
+
+    def step():
+        A.copy_(A_master)
+        mak.qr_compact_(A, (Q, R), alg)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    clocks = ClockSampler(str(torch.cuda.get_device_properties(dev).uuid))
+    clocks.start()
+    launches0 = lib.mak_kernel_launches()
+    lib.mak_profile_start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    barrier()
+    lib.mak_profile_stop()
+    clk = clocks.stop()
+    launches = int(lib.mak_kernel_launches() - launches0)
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    flops = qr_flops(m, n)
+    value = ws * flops / (ms / 1e3) / 1e12
+
+    # dominant kernel: device time of every GEMM launch inside the timed region
+    kind = 1 if args.precision == "mixed" else 0
+    g_ms, g_work, g_cnt = C.c_double(), C.c_double(), C.c_uint64()
+    lib.mak_profile_read(kind, C.byref(g_ms), C.byref(g_work), C.byref(g_cnt))
+    p_ms, p_work, p_cnt = C.c_double(), C.c_double(), C.c_uint64()
+    lib.mak_profile_read(2, C.byref(p_ms), C.byref(p_work), C.byref(p_cnt))
+    breakdown = {}
+    for kname, kid in (("gemm_native", 0), ("gemm_split_tensor", 1), ("qr_panel", 2)):
+        k_ms, k_work, k_cnt = C.c_double(), C.c_double(), C.c_uint64()
+        lib.mak_profile_read(kid, C.byref(k_ms), C.byref(k_work), C.byref(k_cnt))
+        breakdown[kname] = {"launches": int(k_cnt.value),
+                            "ms_per_step": round(k_ms.value / args.steps, 3)}
+
+    # accuracy of the last result (checker: torch/cuBLAS FP64, outside timing)
+    res = orth_abs = orth_rel = diag_ok = None
+    if not args.lean:
+        An = torch.linalg.norm(A_master)
+        res = float(torch.linalg.norm(A_master - Q @ R) / An)
+        G = Q.mT.conj() @ Q
+        orth_abs = float(torch.linalg.norm(G - torch.eye(G.shape[0], dtype=G.dtype, device=dev)))
+        orth_rel = orth_abs / float(torch.linalg.norm(G))
+        del G
+        diag_ok = bool((torch.diagonal(R) >= 0).all())
+
+    # measured FP64 peak (cuBLAS DGEMM 8192^3, best of 5) for the native roofline
+    peaks = {}
+    pk_path = ROOT / "MEASURED_PEAKS.json"
+    if pk_path.exists():
+        peaks = json.loads(pk_path.read_text())
+    if kind == 0 and args.lean:
+        peak, peak_src = None, "not measured (--lean)"
+    elif kind == 0:
+        X = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+        best = 1e30
+        for _ in range(6):
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record()
+            X @ X
+            s1.record()
+            torch.cuda.synchronize()
+            best = min(best, s0.elapsed_time(s1))
+        del X
+        peak = 2 * 8192 ** 3 / (best / 1e3) / 1e12
+        peak_src = "cuBLAS DGEMM 8192^3 measured in this run (FP64 has no MEASURED_PEAKS entry)"
+    else:
+        peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
+        peak_src = ("MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else
+                    "fallback 1.7 PFLOP/s sustained bf16")
+    # native: FP64 flops of the products; mixed: the bf16 tensor-core flops the
+    # split method performs (45 plane products per FP64 product, 9 slices)
+    tensor_work = g_work.value * (OZ_PAIRS if kind == 1 else 1)
+    achieved = tensor_work / (g_ms.value / 1e3) / 1e12 if g_ms.value > 0 else 0.0
+    fp64_equiv = g_work.value / (g_ms.value / 1e3) / 1e12 if g_ms.value > 0 else 0.0
+    roofline = {"bound": "tensor", "achieved": round(achieved, 4), "peak": round(peak, 4),
+                "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
+                "fp64_equivalent_tflops": round(fp64_equiv, 4),
+                "traffic": None,
+                "kernel": "gemm_kernel<double> (larfb / orgqr products)" if kind == 0
+                else "ozaki_gemm (split-bf16 tcgen05)",
+                "launches": int(g_cnt.value), "avg_launch_ms": round(g_ms.value / max(1, g_cnt.value), 4),
+                "share_of_step": round(g_ms.value / (ms * args.steps), 4),
+                "peak_source": peak_src,
+                "panel": {"launches": int(p_cnt.value), "ms_total": round(p_ms.value, 3),
+                          "achieved_gbs": round(p_work.value / (p_ms.value / 1e3) / 1e9, 2)
+                          if p_ms.value > 0 else None},
+                "breakdown": breakdown}
+
+    out = {
+        "metric": METRIC, "value": round(value, 5), "unit": "TFLOP/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic iid N(0,1) (numpy default_rng, seed %d)" % SEED,
+        "config": config_of(args),
+        "factorizations_per_s": round(ws * 1e3 / ms, 4),
+        "accuracy": {"qr_residual": res, "orth_abs_fro": orth_abs,
+                     "orth_rel": orth_rel, "diag_R_nonnegative": diag_ok},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "clocks": clk,
+    }
+
+    # end-to-end through the public API with host buffers
+    if not args.no_e2e and not args.lean:
+        A_pin = torch.empty((n, m), dtype=torch.float64).pin_memory().t()
+        A_pin.copy_(A_host)
+        Q_pin = torch.empty((Q.shape[1], Q.shape[0]), dtype=torch.float64).pin_memory().t()
+        R_pin = torch.empty((R.shape[1], R.shape[0]), dtype=torch.float64).pin_memory().t()
+
+        def e2e_step():
+            A.copy_(A_pin, non_blocking=True)
+            mak.qr_compact_(A, (Q, R), alg)
+            Q_pin.copy_(Q, non_blocking=True)
+            R_pin.copy_(R, non_blocking=True)
+
+        e2e_step()
+        barrier()
+        k2 = max(1, min(args.steps, 3))
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        for _ in range(k2):
+            e2e_step()
+        s1.record()
+        barrier()
+        ems = s0.elapsed_time(s1) / k2
+        if dist is not None:
+            t = torch.tensor([ems], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        out["e2e"] = {"value": round(ws * flops / (ems / 1e3) / 1e12, 5), "unit": "TFLOP/s",
+                      "ms_per_step": round(ems, 3), "steps": k2,
+                      "h2d_bytes_per_step": int(A.numel() * 8),
+                      "d2h_bytes_per_step": int((Q.numel() + R.numel()) * 8)}
+        del A_pin, Q_pin, R_pin
+
+    # left_polar! (Newton) on the single large polar problem
+    if not args.no_polar and not args.lean:
+        out["polar"] = polar_measure(mak, args, dev)
+
+    if rank == 0 and not args.no_cpu_baseline and not args.lean:
+        ms_, ns_ = (int(x) for x in args.cpu_sample.split("x"))
+        rate, t, cores = cpu_qr_rate(ms_, ns_)
+        out["cpu_baseline"] = {"value": round(rate, 5), "unit": "TFLOP/s", "cores": cores,
+                               "kind": "port",
+                               "sample": f"one qr_compact positive=true {ms_}x{ns_} Float64 "
+                                         f"(LAPACK ?geqrt nb=36 + ?gemqrt + gaugefix), "
+                                         f"{t:.2f} s"}
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+def polar_measure(mak, args, dev):
+    import numpy as np
+    import torch
+
+    n = args.polar_n
+    rng = np.random.default_rng(SEED + 7)
+
+    def haar(k):
+        G = rng.standard_normal((k, k))
+        Qh, Rh = np.linalg.qr(G)
+        return Qh * np.sign(np.diagonal(Rh))[None, :]
+
+    U, V = haar(n), haar(n)
+    s = np.logspace(0, -6, n)
+    A_np = (U * s[None, :]) @ V.T
+    A0 = torch.from_numpy(np.asfortranarray(A_np)).to(dev)
+    A = torch.empty_like(A0)
+    W, P = mak.polar.initialize_output(A0)
+    alg = mak.GB300_PolarNewton(precision=args.precision)
+    info = {}
+    A.copy_(A0)
+    mak.left_polar_(A, (W, P), alg, _info=info)  # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    A.copy_(A0)
+    mak.left_polar_(A, (W, P), alg, _info=info)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    k = info["iterations"]
+    back = float(torch.linalg.norm(A0 - W @ P) / torch.linalg.norm(A0))
+    G = W.mT @ W
+    orth = float(torch.linalg.norm(G - torch.eye(n, dtype=G.dtype, device=dev)))
+    return {"workload": f"left_polar! PolarNewton, {n}x{n} Float64, U diag(logspace(0,-6)) V^T",
+            "precision": args.precision, "ms": round(ms, 2), "iterations": k,
+            "tflops": round(polar_flops(n, n, k) / (ms / 1e3) / 1e12, 4),
+            "flop_count": "k*8n^3/3 + 2n^3 (reference PolarNewton count with its own k)",
+            "back_err": back, "orth_abs_fro": orth, "orth_rel": orth / math.sqrt(n),
+            "steps": 1, "warmup": 1}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -140,6 +140,27 @@ int mak_qr_full_c(int64_t m, int64_t n, void* A, int64_t lda, void* Q, int64_t l
                   void* R, int64_t ldr, const mak_qr_opts* opts, void* work,
                   size_t work_bytes, mak_info* info, mak_stream_t stream);
 
+/* ----------------------------------------------------------------- GEMM ---
+ * C = alpha op(A) op(B) + beta C, op in {0: N, 1: T, 2: C (conjugate
+ * transpose)}.  The product kernel every factorization above uses, exposed
+ * so callers can run their own contractions with the same precision control
+ * (reference: the mul! calls of src/implementations/polar.jl:63,108,163 and
+ * src/pullbacks/{qr,polar}.jl, which go to cuBLAS through CUDA.jl).
+ * precision = MAK_PREC_MIXED: Float64 data is split into seven 7-bit bf16
+ * digit planes and multiplied on the tcgen05 tensor cores with exact fp32
+ * group accumulation (Ozaki scheme); alpha/beta must then be real.
+ */
+int mak_gemm_workspace(int dtype, int opA, int opB, int64_t m, int64_t n, int64_t k,
+                       int precision, size_t* bytes);
+int mak_gemm_d(int opA, int opB, int64_t m, int64_t n, int64_t k, double alpha, const double* A,
+               int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+               int precision, void* work, size_t work_bytes, mak_info* info,
+               mak_stream_t stream);
+int mak_gemm_z(int opA, int opB, int64_t m, int64_t n, int64_t k, const double* alpha,
+               const void* A, int64_t lda, const void* B, int64_t ldb, const double* beta,
+               void* C, int64_t ldc, int precision, void* work, size_t work_bytes,
+               mak_info* info, mak_stream_t stream);
+
 /* ---------------------------------------------------------------- polar ---
  * left_polar!(A, (W, P), GB300_PolarNewton(; maxiter, tol))
  * Replaces the reference's left_polar!(::PolarNewton) + left_polar_newton!
@@ -166,6 +187,68 @@ int mak_left_polar_newton_s(int64_t m, int64_t n, float* A, int64_t lda, float* 
 int mak_left_polar_newton_c(int64_t m, int64_t n, void* A, int64_t lda, void* W, int64_t ldw,
                             void* P, int64_t ldp, const mak_polar_opts* opts, void* work,
                             size_t work_bytes, mak_info* info, mak_stream_t stream);
+
+/* ------------------------------------------------------------ pullbacks ---
+ * qr_pullback!(dA, A, (Q, R), (dQ, dR); rank_atol, gauge_atol)
+ * Replaces the reference's qr_pullback! (src/pullbacks/qr.jl:73-120) with
+ * check_and_prepare_qr_cotangents (qr.jl:4-53) and qr_rank (qr.jl:1-2).
+ * full = 0: Q m x min(m,n), R min(m,n) x n (qr_compact); full = 1: Q m x m,
+ * R m x n (qr_full).  dA (m x n) is ACCUMULATED into (dA += ...).  dQ and/or
+ * dR may be NULL (a zero tangent).  info->rank = the numerical rank p used,
+ * info->gauge / gauge_atol = the gauge-dependent cotangent size and the
+ * tolerance the reference warns against.  Synchronizes `stream` once (to
+ * read p, which fixes the shapes of the products).
+ */
+int mak_qr_pullback_workspace(int dtype, int64_t m, int64_t n, int full, int precision,
+                              size_t* bytes);
+int mak_qr_pullback_d(int64_t m, int64_t n, int full, double* dA, int64_t ldda, const double* Q,
+                      int64_t ldq, const double* R, int64_t ldr, const double* dQ, int64_t lddq,
+                      const double* dR, int64_t lddr, const mak_pullback_opts* opts, void* work,
+                      size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_qr_pullback_z(int64_t m, int64_t n, int full, void* dA, int64_t ldda, const void* Q,
+                      int64_t ldq, const void* R, int64_t ldr, const void* dQ, int64_t lddq,
+                      const void* dR, int64_t lddr, const mak_pullback_opts* opts, void* work,
+                      size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_qr_pullback_s(int64_t m, int64_t n, int full, float* dA, int64_t ldda, const float* Q,
+                      int64_t ldq, const float* R, int64_t ldr, const float* dQ, int64_t lddq,
+                      const float* dR, int64_t lddr, const mak_pullback_opts* opts, void* work,
+                      size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_qr_pullback_c(int64_t m, int64_t n, int full, void* dA, int64_t ldda, const void* Q,
+                      int64_t ldq, const void* R, int64_t ldr, const void* dQ, int64_t lddq,
+                      const void* dR, int64_t lddr, const mak_pullback_opts* opts, void* work,
+                      size_t work_bytes, mak_info* info, mak_stream_t stream);
+
+/* left_polar_pullback!(dA, A, (W, P), (dW, dP))
+ * Replaces the reference's left_polar_pullback! (src/pullbacks/polar.jl:7-29),
+ * including the Sylvester solve P C + C P = M - M^H (src/common/pullbacks.jl:15),
+ * which the reference's CUDA extension runs on the host
+ * (ext/MatrixAlgebraKitCUDAExt/MatrixAlgebraKitCUDAExt.jl:193-198); here it is
+ * a device sign-function Newton iteration.  dA is accumulated into; dW / dP
+ * may be NULL.  info->iterations = sign iterations.  Synchronizes `stream`
+ * once per sign iteration (stopping test).
+ */
+int mak_left_polar_pullback_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                      size_t* bytes);
+int mak_left_polar_pullback_d(int64_t m, int64_t n, double* dA, int64_t ldda, const double* W,
+                              int64_t ldw, const double* P, int64_t ldp, const double* dW,
+                              int64_t lddw, const double* dP, int64_t lddp,
+                              const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                              mak_info* info, mak_stream_t stream);
+int mak_left_polar_pullback_z(int64_t m, int64_t n, void* dA, int64_t ldda, const void* W,
+                              int64_t ldw, const void* P, int64_t ldp, const void* dW,
+                              int64_t lddw, const void* dP, int64_t lddp,
+                              const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                              mak_info* info, mak_stream_t stream);
+int mak_left_polar_pullback_s(int64_t m, int64_t n, float* dA, int64_t ldda, const float* W,
+                              int64_t ldw, const float* P, int64_t ldp, const float* dW,
+                              int64_t lddw, const float* dP, int64_t lddp,
+                              const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                              mak_info* info, mak_stream_t stream);
+int mak_left_polar_pullback_c(int64_t m, int64_t n, void* dA, int64_t ldda, const void* W,
+                              int64_t ldw, const void* P, int64_t ldp, const void* dW,
+                              int64_t lddw, const void* dP, int64_t lddp,
+                              const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                              mak_info* info, mak_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -21,6 +21,7 @@ from . import _lib
 from .algorithms import (ArgumentError, DimensionMismatch, GB300_HouseholderQR,
                          GB300_PolarNewton, LeftOrthViaPolar, LeftOrthViaQR, default_algorithm,
                          is_positive, select_algorithm)
+from .blas import gemm
 from .polar import SingularException, left_polar, left_polar_
 from .qr import (initialize_output, qr_compact, qr_compact_, qr_full, qr_full_, qr_null,
                  qr_null_)
@@ -29,10 +30,14 @@ __all__ = [
     "ArgumentError", "DimensionMismatch", "SingularException", "GB300_HouseholderQR",
     "GB300_PolarNewton", "LeftOrthViaQR", "LeftOrthViaPolar", "default_algorithm",
     "select_algorithm", "is_positive", "qr_compact", "qr_compact_", "qr_full", "qr_full_",
-    "qr_null", "qr_null_", "left_polar", "left_polar_", "initialize_output", "library",
+    "qr_null", "qr_null_", "left_polar", "left_polar_", "initialize_output", "library", "gemm",
 ]
 
 
 def library():
     """The loaded ctypes handle of libmak_gb300.so (raises if unavailable)."""
     return _lib.load()
+
+from .pullbacks import left_polar_pullback_, qr_pullback_  # noqa: E402
+
+__all__ += ["qr_pullback_", "left_polar_pullback_"]

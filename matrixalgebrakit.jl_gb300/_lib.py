@@ -59,7 +59,27 @@ _QR_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, C.POINTER(mak_qr_opts), _p
 for _kind in ("compact", "full"):
     for _s in "dzsc":
         SIGNATURES[f"mak_qr_{_kind}_{_s}"] = (C.c_int, _QR_ARGS)
-SIGNATURES["mak_left_polar_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
+SIGNATURES["mak_gemm_workspace"] = (C.c_int, [C.c_int, C.c_int, C.c_int, _i64, _i64, _i64, C.c_int,
+                                              C.POINTER(_sz)])
+SIGNATURES["mak_gemm_d"] = (C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, C.c_double, _p, _i64, _p,
+                                      _i64, C.c_double, _p, _i64, C.c_int, _p, _sz, _p, _p])
+SIGNATURES["mak_gemm_z"] = (C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, C.POINTER(C.c_double), _p,
+                                      _i64, _p, _i64, C.POINTER(C.c_double), _p, _i64, C.c_int, _p,
+                                      _sz, _p, _p])
+SIGNATURES["mak_qr_pullback_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int, C.c_int,
+                                                     C.POINTER(_sz)])
+SIGNATURES["mak_left_polar_pullback_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
+                                                             C.POINTER(_sz)])
+for _s in "dzsc":
+    SIGNATURES[f"mak_qr_pullback_{_s}"] = (C.c_int, [_i64, _i64, C.c_int, _p, _i64, _p, _i64, _p,
+                                                     _i64, _p, _i64, _p, _i64,
+                                                     C.POINTER(mak_pullback_opts), _p, _sz, _p,
+                                                     _p])
+    SIGNATURES[f"mak_left_polar_pullback_{_s}"] = (C.c_int, [_i64, _i64, _p, _i64, _p, _i64, _p,
+                                                             _i64, _p, _i64, _p, _i64,
+                                                             C.POINTER(mak_pullback_opts), _p,
+                                                             _sz, _p, _p])
+SIGNATURES["mak_left_polar_workspace"] =(C.c_int, [C.c_int, _i64, _i64, C.c_int,
                                                     C.POINTER(mak_polar_opts), C.POINTER(_sz)])
 _POLAR_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, C.POINTER(mak_polar_opts), _p, _sz, _p,
                _p]

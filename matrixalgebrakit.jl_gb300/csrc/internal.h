@@ -25,3 +25,23 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
 int info_reset(cudaStream_t st, mak_info* info);
 
 }  // namespace mak
+
+#include "gemm.cuh"
+
+namespace mak {
+
+// Split-precision (Ozaki scheme, bf16 tcgen05) GEMM for Float64 / ComplexF64:
+// C = alpha op(A) op(B) + beta C with real alpha, beta.  Workspace from `ar`
+// (measured when ar.base == nullptr).
+template <class T>
+int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T> A, Operand<T> B,
+            T beta, T* C, int64_t ldc, Arena& ar, int* status);
+
+// Dispatch: the tensor-core split GEMM when `precision` is MAK_PREC_MIXED and
+// the element type is a Float64 type with real alpha/beta, else the native
+// SIMT GEMM.  `ar` supplies the split planes (sized by a measuring pass).
+template <class T>
+int gemm_prec(cudaStream_t st, int precision, int64_t M, int64_t N, int64_t K, T alpha,
+              Operand<T> A, Operand<T> B, T beta, T* C, int64_t ldc, Arena& ar, int* status);
+
+}  // namespace mak

@@ -32,6 +32,7 @@
 namespace mak {
 
 constexpr int GJ_NB = 32;
+constexpr int GJ_OUTER_NB = 128;  // block column of the mixed-precision path
 constexpr int GJ_THREADS = 256;
 
 template <class T>
@@ -153,11 +154,12 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
 
 // For every column outside the panel: apply the panel's row exchanges in
 // order, save rows k0..k0+b-1 into buf (b x n) and zero them in X.
+// Only columns c in [c_lo, c_hi) are touched.
 template <class T>
 __global__ void gje_laswp_save_kernel(int n, T* X, int64_t ldx, int k0, int b, const int* piv,
-                                      T* buf) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n || (c >= k0 && c < k0 + b)) return;
+                                      T* buf, int c_lo, int c_hi) {
+  const int c = c_lo + blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= c_hi || (c >= k0 && c < k0 + b)) return;
   T* col = X + (int64_t)c * ldx;
   for (int t = 0; t < b; t++) {
     const int jj = k0 + t, p = piv[jj];
@@ -217,14 +219,28 @@ static size_t gj_slab_cap() {
 template <class T>
 int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int precision,
                 Arena& ar, mak_info* info) {
-  (void)precision;
   const int sms = num_sms();
+  // mixed precision: 128-wide block columns, eliminated with 32-wide panels
+  // whose updates stay inside the block; the other columns then receive one
+  // rank-128 update through the split-precision tensor-core GEMM
+  const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8;
+  const int NBO = mixed ? GJ_OUTER_NB : GJ_NB;
   int* piv = ar.take<int>(n > 0 ? n : 1);
   real_t<T>* part_val = ar.take<real_t<T>>(sms);
   int* part_idx = ar.take<int>(sms);
   T* swapbuf = ar.take<T>(2 * GJ_NB);
-  T* buf = ar.take<T>((size_t)GJ_NB * (n > 0 ? n : 1));
+  T* buf = ar.take<T>((size_t)NBO * (n > 0 ? n : 1));
+  T* bufo = mixed ? ar.take<T>((size_t)NBO * (n > 0 ? n : 1)) : nullptr;
   unsigned* bar = ar.take<unsigned>(2);
+  char* ozs = nullptr;
+  size_t oz_bytes = 0;
+  if (mixed) {
+    Arena meas(nullptr, 0);
+    gemm_prec<T>(st, precision, n, n, NBO, one_<T>(), opnd<T>(nullptr, 1), opnd<T>(nullptr, 1),
+                 one_<T>(), nullptr, 1, meas, nullptr);
+    oz_bytes = meas.off + 1024;
+    ozs = ar.take<char>(oz_bytes);
+  }
   if (ar.base == nullptr) return 0;
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
   if (n <= 0) return 0;
@@ -237,6 +253,9 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
   const size_t cap = gj_slab_cap<T>();
   for (int64_t k0 = 0; k0 < n; k0 += GJ_NB) {
     const int b = (int)((n - k0) < GJ_NB ? (n - k0) : GJ_NB);
+    const int64_t K0 = (k0 / NBO) * NBO;  // enclosing block column
+    const int64_t KB = (n - K0) < NBO ? (n - K0) : NBO;
+    const int64_t c_lo = mixed ? K0 : 0, c_hi = mixed ? K0 + KB : n;
     // grid: rows per CTA >= 64, one CTA per SM, slab within shared memory
     int64_t G = ceil_div(n, 64);
     if (G > sms) G = sms;
@@ -252,21 +271,42 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
     GjArgs<T> ga{X, ldx, (int)n, (int)k0, b, (int)rpc, piv, part_val, part_idx, swapbuf,
                  bar, &info->status, &info->singular};
     void* args[] = {&ga};
-    ProfScope prof(st, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
+    {
+      ProfScope prof(st, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
+      note_launch();
+      MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)gje_panel_kernel<T>, dim3((unsigned)G),
+                                               dim3(GJ_THREADS), args, smem, st));
+    }
     note_launch();
-    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)gje_panel_kernel<T>, dim3((unsigned)G),
-                                             dim3(GJ_THREADS), args, smem, st));
-    note_launch();
-    gje_laswp_save_kernel<T><<<(unsigned)ceil_div(n, 128), 128, 0, st>>>((int)n, X, ldx, (int)k0,
-                                                                         b, piv, buf);
+    gje_laswp_save_kernel<T><<<(unsigned)ceil_div(c_hi - c_lo, 128), 128, 0, st>>>(
+        (int)n, X, ldx, (int)k0, b, piv, buf, (int)c_lo, (int)c_hi);
     MAK_CUDA_TRY(cudaGetLastError());
     const T* F = X + k0 * ldx;
-    if (k0 > 0)
-      MAK_TRY(gemm<T>(st, n, k0, b, one_<T>(), opnd<T>(F, ldx), opnd<T>(buf, b), one_<T>(), X,
-                      ldx));
-    if (k0 + b < n)
-      MAK_TRY(gemm<T>(st, n, n - k0 - b, b, one_<T>(), opnd<T>(F, ldx),
+    if (k0 > c_lo)
+      MAK_TRY(gemm<T>(st, n, k0 - c_lo, b, one_<T>(), opnd<T>(F, ldx),
+                      opnd<T>(buf + c_lo * b, b), one_<T>(), X + c_lo * ldx, ldx));
+    if (k0 + b < c_hi)
+      MAK_TRY(gemm<T>(st, n, c_hi - k0 - b, b, one_<T>(), opnd<T>(F, ldx),
                       opnd<T>(buf + (k0 + b) * b, b), one_<T>(), X + (k0 + b) * ldx, ldx));
+    if (mixed && k0 + b == K0 + KB) {
+      // block column finished: exchanges + rank-KB update of the other columns
+      note_launch();
+      gje_laswp_save_kernel<T><<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(
+          (int)n, X, ldx, (int)K0, (int)KB, piv, bufo, 0, (int)n);
+      MAK_CUDA_TRY(cudaGetLastError());
+      const T* Fb = X + K0 * ldx;
+      if (K0 > 0) {
+        Arena oz(ozs, oz_bytes);
+        MAK_TRY(gemm_prec<T>(st, precision, n, K0, KB, one_<T>(), opnd<T>(Fb, ldx),
+                             opnd<T>(bufo, KB), one_<T>(), X, ldx, oz, &info->status));
+      }
+      if (K0 + KB < n) {
+        Arena oz(ozs, oz_bytes);
+        MAK_TRY(gemm_prec<T>(st, precision, n, n - K0 - KB, KB, one_<T>(), opnd<T>(Fb, ldx),
+                             opnd<T>(bufo + (K0 + KB) * KB, KB), one_<T>(),
+                             X + (K0 + KB) * ldx, ldx, oz, &info->status));
+      }
+    }
   }
   note_launch();
   gje_perm_kernel<<<1, 1024, (size_t)n * sizeof(int), st>>>((int)n, piv, iperm);

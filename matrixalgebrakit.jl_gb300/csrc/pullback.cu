@@ -1,0 +1,598 @@
+// Reverse-mode rules of the QR and left polar decompositions, GB300 native.
+//
+// qr_pullback (reference src/pullbacks/qr.jl:1-120):
+//   p   = last j with |R_jj| >= rank_atol   (rank_atol = eps(max|R|)^(3/4))
+//   gauge check of the cotangents (qr.jl:4-53), reported in info->gauge
+//   dQ1 -= Q1 (dR12 R12^H);  dA2 += Q1 dR12                       (n > p)
+//   M    = triu(dR11) R11^H - Q1^H dQ1;  M <- copyltu(M), real diagonal
+//   dQ1 += Q1 M;             dA1 += dQ1 R11^{-H}
+//   The triangular solve uses the explicit inverse of R11 from the
+//   Gauss-Jordan kernel (no pivot exchanges occur on a triangular matrix).
+//
+// left_polar_pullback (reference src/pullbacks/polar.jl:7-29):
+//   dP <- herm(dP);  M = W^H dW - dP P;  solve P C + C P = M - M^H;
+//   C += dP;  dA += W C;  dA += (I - W W^H) dW P^{-1}
+//   The Sylvester equation is solved on the device (the reference's CUDA
+//   extension copies P to the host for LAPACK trsyl,
+//   ext/MatrixAlgebraKitCUDAExt/MatrixAlgebraKitCUDAExt.jl:193-198) by the
+//   Newton iteration for the matrix sign function of H = [[P, -B], [0, -P]]:
+//   sign(H) = [[I, -2X], [0, -I]] with P X + X P = B.  With
+//   H_k = [[A_k, C_k], [0, -A_k]] the iteration decouples into
+//     A_{k+1} = (mu A_k + A_k^{-1}/mu)/2,
+//     C_{k+1} = (mu C_k + A_k^{-1} C_k A_k^{-1}/mu)/2,
+//   A_0 = P, C_0 = -B, mu = sqrt(||A_k^{-1}||_F / ||A_k||_F); X = -C_inf/2.
+//   Only GEMMs and the Gauss-Jordan inverse are needed (no eigensolver).
+#include "gemm.cuh"
+#include "internal.h"
+#include "util.cuh"
+
+namespace mak {
+
+// ---------------------------------------------------------------- helpers --
+// eps(x)^(3/4) of Julia (`eps(x)` = spacing of floats at x)
+template <class R>
+__device__ __forceinline__ R eps34(R x) {
+  if (!(x > R(0))) return R(0);
+  int e;
+  frexp(x, &e);  // x = f 2^e, f in [0.5, 1)
+  const int mant = sizeof(R) == 8 ? 52 : 23;
+  const R sp = ldexp(R(1), e - 1 - mant);
+  return pow(sp, R(0.75));
+}
+
+// p = 1 + last j < k with |R_jj| >= atol (atol < 0: eps(maxR)^(3/4)); 0 if none
+template <class T>
+__global__ void qr_rank_kernel(int k, const T* R, int64_t ldr, const real_t<T>* maxR,
+                               double atol_in, int* p_out, real_t<T>* atol_out) {
+  using Rr = real_t<T>;
+  __shared__ int best[32];
+  const Rr atol = atol_in >= 0 ? (Rr)atol_in : eps34(*maxR);
+  int b = 0;
+  for (int j = threadIdx.x; j < k; j += blockDim.x)
+    if (abs_(R[j + (int64_t)j * ldr]) >= atol) b = j + 1 > b ? j + 1 : b;
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    int o = __shfl_xor_sync(0xffffffffu, b, m);
+    b = o > b ? o : b;
+  }
+  if ((threadIdx.x & 31) == 0) best[threadIdx.x >> 5] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int r = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = best[w] > r ? best[w] : r;
+    *p_out = r;
+    if (atol_out) *atol_out = atol;
+  }
+}
+
+// max over the upper triangle (incl. diagonal) of X (rows x cols) -> *out (max-combine)
+template <class T>
+__global__ void max_upper_kernel(int rows, int cols, const T* X, int64_t ldx, real_t<T>* out) {
+  using Rr = real_t<T>;
+  __shared__ Rr sh[32];
+  Rr mx = Rr(0);
+  const int64_t total = (int64_t)rows * cols;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e % rows), j = (int)(e / rows);
+    if (i <= j) mx = fmax(mx, abs_(X[i + (int64_t)j * ldx]));
+  }
+  mx = block_max(mx, sh);
+  if (threadIdx.x == 0) {
+    // non-negative reals compare like their bit patterns
+    if (sizeof(Rr) == 8)
+      atomicMax((unsigned long long*)out, (unsigned long long)__double_as_longlong((double)mx));
+    else
+      atomicMax((unsigned int*)out, __float_as_uint((float)mx));
+  }
+}
+
+// M <- copyltu(M): lower triangle = conj(upper), real diagonal (qr.jl:108-112)
+template <class T>
+__global__ void copyltu_kernel(int p, T* M, int64_t ldm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= p || j >= p) return;
+  if (i > j) M[i + (int64_t)j * ldm] = conj_(M[j + (int64_t)i * ldm]);
+  else if (i == j) M[i + (int64_t)i * ldm] = make_scalar<T>(re_(M[i + (int64_t)i * ldm]), 0);
+}
+
+// B = s (M - M^H)   (n x n, out of place)
+template <class T>
+__global__ void antiherm_kernel(int n, const T* M, int64_t ldm, real_t<T> s, T* B, int64_t ldb) {
+  __shared__ T t[32][33];
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < 32; r += 8) {
+    const int i = j0 + tx, j = i0 + r;  // load M[j0+tx, i0+r] -> t[r][tx]
+    t[r][tx] = (i < n && j < n) ? M[i + (int64_t)j * ldm] : zero_<T>();
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, j = j0 + r;
+    if (i < n && j < n) B[i + (int64_t)j * ldb] = s * (M[i + (int64_t)j * ldm] - conj_(t[tx][r]));
+  }
+}
+
+// Y[:, c] = X[:, iperm[c]]  (explicit inverse from the Gauss-Jordan output)
+template <class T>
+__global__ void gather_cols_kernel(int n, const T* X, int64_t ldx, const int* iperm, T* Y,
+                                   int64_t ldy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (i < n && c < n) Y[i + (int64_t)c * ldy] = X[i + (int64_t)iperm[c] * ldx];
+}
+
+// sign-iteration update, mu = (||Ai||^2/||A||^2)^(1/4):
+//   A <- (mu A + Ai/mu)/2,  C <- (mu C + Tm/mu)/2,  *dnorm += |A_new - A_old|^2 (partial)
+template <class T>
+__global__ void sign_update_kernel(int64_t nn, T* A, const T* Ai, T* Cm, const T* Tm,
+                                   const real_t<T>* nrm2, real_t<T>* dpart) {
+  using Rr = real_t<T>;
+  __shared__ Rr sh[32];
+  const Rr mu = sqrt(sqrt(nrm2[1] / nrm2[0]));
+  const Rr imu = Rr(1) / mu;
+  Rr acc = Rr(0);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const T a = A[e];
+    const T an = Rr(0.5) * (mu * a + imu * Ai[e]);
+    A[e] = an;
+    acc += abs2_(an - a);
+    Cm[e] = Rr(0.5) * (mu * Cm[e] + imu * Tm[e]);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) dpart[blockIdx.x] = acc;
+}
+
+template <class R>
+__global__ void eps34_kernel(const R* x, R* out) {
+  *out = eps34(*x);
+}
+
+// Y[0:m, 0:n] += X (both strided)
+template <class T>
+__global__ void add_strided_kernel(int64_t m, int64_t n, const T* X, int64_t ldx, T* Y,
+                                   int64_t ldy) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y)
+    if (i < m) Y[i + j * ldy] += X[i + j * ldx];
+}
+
+template <class T>
+__global__ void scale_copy_kernel(int64_t nn, const T* X, real_t<T> s, T* Y) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nn) Y[e] = s * X[e];
+}
+template <class T>
+__global__ void add_kernel(int64_t nn, const T* X, T* Y) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nn) Y[e] += X[e];
+}
+
+template <class T>
+__global__ void info_pullback_kernel(mak_info* info, int p, int iters, const real_t<T>* gauge,
+                                     const real_t<T>* gauge_atol) {
+  info->rank = p;
+  info->iterations = iters;
+  info->gauge = gauge ? (double)*gauge : 0.0;
+  info->gauge_atol = gauge_atol ? (double)*gauge_atol : 0.0;
+}
+
+// -------------------------------------------------------------- QR pullback --
+template <class T>
+int qr_pullback_run(cudaStream_t st, int64_t m, int64_t n, int full, T* dA, int64_t ldda,
+                    const T* Q, int64_t ldq, const T* R, int64_t ldr, const T* dQ, int64_t lddq,
+                    const T* dR, int64_t lddr, double rank_atol, double gauge_atol, int precision,
+                    Arena& ar, mak_info* info) {
+  using Rr = real_t<T>;
+  const int64_t k = m < n ? m : n;
+  const int64_t qc = full ? m : k;
+  Rr* scal = ar.take<Rr>(RED_CTAS + 16);  // reductions + scalars
+  int* pdev = ar.take<int>(4);
+  T* dQ1 = ar.take<T>((size_t)m * (k > 0 ? k : 1));
+  T* X = ar.take<T>((size_t)(k > 0 ? k : 1) * (k > 0 ? k : 1));
+  T* Mm = ar.take<T>((size_t)(k > 0 ? k : 1) * (k > 0 ? k : 1));
+  T* Rinv = ar.take<T>((size_t)(k > 0 ? k : 1) * (k > 0 ? k : 1));
+  int* iperm = ar.take<int>(k + 1);
+  T* Q1dQ3 = (full && qc > k) ? ar.take<T>((size_t)k * (qc - k)) : nullptr;
+  T* dQ3 = (full && qc > k) ? ar.take<T>((size_t)m * (qc - k)) : nullptr;
+  size_t gj_ws = 0, oz_ws = 0;
+  {
+    Arena meas(nullptr, 0);
+    gje_inverse<T>(st, k, nullptr, k, nullptr, precision, meas, nullptr);
+    gj_ws = meas.off + 256;
+    const int64_t shapes[4][3] = {{k, k, n}, {m, n, k}, {k, k, m}, {m, k, k}};
+    for (auto& sh : shapes) {
+      Arena m2(nullptr, 0);
+      gemm_prec<T>(st, precision, sh[0], sh[1], sh[2], one_<T>(), opnd<T>(nullptr, 1),
+                   opnd<T>(nullptr, 1), zero_<T>(), nullptr, 1, m2, nullptr);
+      if (m2.off + 256 > oz_ws) oz_ws = m2.off + 256;
+    }
+  }
+  const size_t tail_bytes = gj_ws > oz_ws ? gj_ws : oz_ws;
+  char* tail = ar.take<char>(tail_bytes);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  int* status = &info->status;
+  Rr* red = scal;
+  Rr* maxR = scal + RED_CTAS;
+  Rr* gauge = scal + RED_CTAS + 1;
+  Rr* gatol = scal + RED_CTAS + 2;
+  Rr* ratol = scal + RED_CTAS + 3;
+  Rr* tmp = scal + RED_CTAS + 4;
+  auto G = [&](int64_t M_, int64_t N_, int64_t K_, T alpha, Operand<T> a, Operand<T> b, T beta,
+               T* C_, int64_t ldc) -> int {
+    Arena oz(tail, tail_bytes);
+    return gemm_prec<T>(st, precision, M_, N_, K_, alpha, a, b, beta, C_, ldc, oz, status);
+  };
+
+  // rank
+  MAK_CUDA_TRY(cudaMemsetAsync(scal + RED_CTAS, 0, 16 * sizeof(Rr), st));
+  MAK_TRY(reduce_mat<T>(st, k, n, R, ldr, 1, red, maxR));
+  note_launch();
+  qr_rank_kernel<T><<<1, 256, 0, st>>>((int)k, R, ldr, maxR, rank_atol, pdev, ratol);
+  MAK_CUDA_TRY(cudaGetLastError());
+  int p = 0;
+  MAK_CUDA_TRY(cudaMemcpyAsync(&p, pdev, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MAK_CUDA_TRY(cudaStreamSynchronize(st));
+
+  // gauge tolerance: eps(max|dQ|)^(3/4) (0 for a zero tangent)
+  if (gauge_atol >= 0) {
+    Rr g = (Rr)gauge_atol;
+    MAK_CUDA_TRY(cudaMemcpyAsync(gatol, &g, sizeof(Rr), cudaMemcpyHostToDevice, st));
+    MAK_CUDA_TRY(cudaStreamSynchronize(st));
+  } else if (dQ) {
+    MAK_TRY(reduce_mat<T>(st, m, qc, dQ, lddq, 1, red, tmp));
+    note_launch();
+    eps34_kernel<Rr><<<1, 1, 0, st>>>(tmp, gatol);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
+
+  // dQ1 (and the qr_full correction of the gauge-invariant part of dQ3)
+  if (dQ) {
+    MAK_TRY(copy_mat<T>(st, m, p, dQ, lddq, dQ1, m));
+    if (p == k && qc > k) {
+      const T* Q3 = Q + k * ldq;
+      const T* dQ3src = dQ + k * lddq;
+      MAK_TRY(copy_mat<T>(st, m, qc - k, dQ3src, lddq, dQ3, m));
+      MAK_TRY(G(k, qc - k, m, one_<T>(), opnd<T>(Q, ldq, OP_C), opnd<T>(dQ3src, lddq), zero_<T>(),
+                Q1dQ3, k));
+      MAK_TRY(G(m, qc - k, k, -one_<T>(), opnd<T>(Q, ldq), opnd<T>(Q1dQ3, k), one_<T>(), dQ3, m));
+      MAK_TRY(reduce_mat<T>(st, m, qc - k, dQ3, m, 1, red, gauge));
+      MAK_TRY(G(m, k, qc - k, -one_<T>(), opnd<T>(Q3, ldq), opnd<T>(Q1dQ3, k, OP_C), one_<T>(),
+                dQ1, m));
+    } else if (qc > p) {
+      MAK_TRY(reduce_mat<T>(st, m, qc - p, dQ + p * lddq, lddq, 1, red, gauge));
+    }
+  } else if (p > 0) {
+    MAK_CUDA_TRY(cudaMemsetAsync(dQ1, 0, (size_t)m * p * sizeof(T), st));
+  }
+  if (dR && p < k) {
+    note_launch();
+    max_upper_kernel<T><<<64, 256, 0, st>>>((int)(k - p), (int)(n - p), dR + p + p * lddr, lddr,
+                                            gauge);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
+
+  if (p > 0) {
+    const T* R12 = R + p * ldr;
+    if (dR && n > p) {
+      const T* dR12 = dR + p * lddr;
+      // X = dR12 R12^H ; dQ1 -= Q1 X ; dA2 += Q1 dR12
+      MAK_TRY(G(p, p, n - p, one_<T>(), opnd<T>(dR12, lddr), opnd<T>(R12, ldr, OP_C), zero_<T>(),
+                X, p));
+      MAK_TRY(G(m, p, p, -one_<T>(), opnd<T>(Q, ldq), opnd<T>(X, p), one_<T>(), dQ1, m));
+      MAK_TRY(G(m, n - p, p, one_<T>(), opnd<T>(Q, ldq), opnd<T>(dR12, lddr), one_<T>(),
+                dA + p * ldda, ldda));
+    }
+    // M = triu(dR11) R11^H - Q1^H dQ1
+    if (dR)
+      MAK_TRY(G(p, p, p, one_<T>(), opnd<T>(dR, lddr, OP_N, MASK_UPPER),
+                opnd<T>(R, ldr, OP_C, MASK_UPPER), zero_<T>(), Mm, p));
+    MAK_TRY(G(p, p, m, -one_<T>(), opnd<T>(Q, ldq, OP_C), opnd<T>(dQ1, m),
+              dR ? one_<T>() : zero_<T>(), Mm, p));
+    note_launch();
+    copyltu_kernel<T><<<dim3((unsigned)ceil_div(p, 128), (unsigned)p), 128, 0, st>>>((int)p, Mm,
+                                                                                      p);
+    MAK_CUDA_TRY(cudaGetLastError());
+    MAK_TRY(G(m, p, p, one_<T>(), opnd<T>(Q, ldq), opnd<T>(Mm, p), one_<T>(), dQ1, m));
+    // dA1 += dQ1 R11^{-H}
+    MAK_TRY(copy_mat<T>(st, p, p, R, ldr, X, p));
+    {
+      Arena gj(tail, tail_bytes);
+      MAK_TRY(gje_inverse<T>(st, p, X, p, iperm, precision, gj, info));
+    }
+    note_launch();
+    gather_cols_kernel<T><<<dim3((unsigned)ceil_div(p, 128), (unsigned)p), 128, 0, st>>>(
+        (int)p, X, p, iperm, Rinv, p);
+    MAK_CUDA_TRY(cudaGetLastError());
+    MAK_TRY(G(m, p, p, one_<T>(), opnd<T>(dQ1, m), opnd<T>(Rinv, p, OP_C, MASK_UPPER), one_<T>(),
+              dA, ldda));
+  }
+  note_launch();
+  info_pullback_kernel<T><<<1, 1, 0, st>>>(info, p, 0, gauge, gatol);
+  MAK_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// ----------------------------------------------------------- polar pullback --
+template <class T>
+int polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldda, const T* W,
+                       int64_t ldw, const T* P, int64_t ldp, const T* dW, int64_t lddw,
+                       const T* dP, int64_t lddp, int maxiter, int precision, Arena& ar,
+                       mak_info* info) {
+  using Rr = real_t<T>;
+  const size_t nn = (size_t)n * n;
+  Rr* scal = ar.take<Rr>(RED_CTAS + 16);
+  T* dPh = ar.take<T>(nn + 1);
+  T* Mm = ar.take<T>(nn + 1);
+  T* Ak = ar.take<T>(nn + 1);
+  T* Ck = ar.take<T>(nn + 1);
+  T* Ai = ar.take<T>(nn + 1);
+  T* Pinv = ar.take<T>(nn + 1);
+  T* Tm = ar.take<T>(nn + 1);
+  T* Y = ar.take<T>((size_t)m * n + 1);
+  int* iperm = ar.take<int>(n + 1);
+  size_t gj_ws = 0, oz_ws = 0;
+  {
+    Arena meas(nullptr, 0);
+    gje_inverse<T>(st, n, nullptr, n, nullptr, precision, meas, nullptr);
+    gj_ws = meas.off + 256;
+    const int64_t shapes[3][3] = {{n, n, m}, {n, n, n}, {m, n, n}};
+    for (auto& sh : shapes) {
+      Arena m2(nullptr, 0);
+      gemm_prec<T>(st, precision, sh[0], sh[1], sh[2], one_<T>(), opnd<T>(nullptr, 1),
+                   opnd<T>(nullptr, 1), zero_<T>(), nullptr, 1, m2, nullptr);
+      if (m2.off + 256 > oz_ws) oz_ws = m2.off + 256;
+    }
+  }
+  const size_t tail_bytes = gj_ws > oz_ws ? gj_ws : oz_ws;
+  char* tail = ar.take<char>(tail_bytes);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  if (n == 0) return 0;
+  int* status = &info->status;
+  Rr* red = scal;
+  Rr* nrm2 = scal + RED_CTAS;  // [0] ||A||^2, [1] ||Ai||^2, [2] ||dA||^2
+  auto G = [&](int64_t M_, int64_t N_, int64_t K_, T alpha, Operand<T> a, Operand<T> b, T beta,
+               T* C_, int64_t ldc) -> int {
+    Arena oz(tail, tail_bytes);
+    return gemm_prec<T>(st, precision, M_, N_, K_, alpha, a, b, beta, C_, ldc, oz, status);
+  };
+  auto inverse = [&](const T* X, T* out) -> int {
+    MAK_TRY(copy_mat<T>(st, n, n, X, n, Tm, n));
+    {
+      Arena gj(tail, tail_bytes);
+      MAK_TRY(gje_inverse<T>(st, n, Tm, n, iperm, precision, gj, info));
+    }
+    note_launch();
+    gather_cols_kernel<T><<<dim3((unsigned)ceil_div(n, 128), (unsigned)n), 128, 0, st>>>(
+        (int)n, Tm, n, iperm, out, n);
+    return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+  };
+  const unsigned g1 = (unsigned)ceil_div((int64_t)nn, 256);
+
+  // dP <- herm(dP);  M = W^H dW - dP P
+  if (dP) {
+    MAK_TRY(copy_mat<T>(st, n, n, dP, lddp, dPh, n));
+    MAK_TRY(herm_project<T>(st, n, dPh, n));
+  }
+  if (dW)
+    MAK_TRY(G(n, n, m, one_<T>(), opnd<T>(W, ldw, OP_C), opnd<T>(dW, lddw), zero_<T>(), Mm, n));
+  else
+    MAK_CUDA_TRY(cudaMemsetAsync(Mm, 0, nn * sizeof(T), st));
+  if (dP)
+    MAK_TRY(G(n, n, n, -one_<T>(), opnd<T>(dPh, n), opnd<T>(P, ldp), one_<T>(), Mm, n));
+  // C_0 = -(M - M^H), A_0 = P
+  {
+    dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+    note_launch();
+    antiherm_kernel<T><<<g, 256, 0, st>>>((int)n, Mm, n, Rr(-1), Ck, n);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
+  MAK_TRY(copy_mat<T>(st, n, n, P, ldp, Ak, n));
+
+  // sign-function Newton iteration
+  const Rr tol = (sizeof(Rr) == 8 ? Rr(1e-13) : Rr(1e-6)) * sqrt((Rr)n);
+  int it = 0;
+  for (it = 1; it <= maxiter; it++) {
+    MAK_TRY(inverse(Ak, Ai));
+    if (it == 1) MAK_TRY(copy_mat<T>(st, n, n, Ai, n, Pinv, n));
+    MAK_TRY(reduce_mat<T>(st, n, n, Ak, n, 0, red, nrm2));
+    MAK_TRY(reduce_mat<T>(st, n, n, Ai, n, 0, red, nrm2 + 1));
+    // Tm = Ai C Ai
+    MAK_TRY(G(n, n, n, one_<T>(), opnd<T>(Ai, n), opnd<T>(Ck, n), zero_<T>(), Y, n));
+    MAK_TRY(G(n, n, n, one_<T>(), opnd<T>(Y, n), opnd<T>(Ai, n), zero_<T>(), Tm, n));
+    const unsigned gr = g1 < RED_CTAS ? g1 : RED_CTAS;
+    note_launch();
+    sign_update_kernel<T><<<gr, 256, 0, st>>>((int64_t)nn, Ak, Ai, Ck, Tm, nrm2, red);
+    MAK_CUDA_TRY(cudaGetLastError());
+    note_launch();
+    reduce_final_kernel<Rr><<<1, 256, 0, st>>>((int)gr, red, 0, nrm2 + 2);
+    MAK_CUDA_TRY(cudaGetLastError());
+    MAK_TRY(herm_project<T>(st, n, Ak, n));
+    Rr dnorm2 = 0;
+    MAK_CUDA_TRY(cudaMemcpyAsync(&dnorm2, nrm2 + 2, sizeof(Rr), cudaMemcpyDeviceToHost, st));
+    MAK_CUDA_TRY(cudaStreamSynchronize(st));
+    if (!(sqrt(dnorm2) > tol)) break;
+  }
+  if (it > maxiter) it = maxiter;
+  // C = -C_inf/2 (+ dP);  dA += W C
+  note_launch();
+  scale_copy_kernel<T><<<g1, 256, 0, st>>>((int64_t)nn, Ck, Rr(-0.5), Tm);
+  MAK_CUDA_TRY(cudaGetLastError());
+  if (dP) {
+    note_launch();
+    add_kernel<T><<<g1, 256, 0, st>>>((int64_t)nn, dPh, Tm);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
+  MAK_TRY(G(m, n, n, one_<T>(), opnd<T>(W, ldw), opnd<T>(Tm, n), one_<T>(), dA, ldda));
+  // dA += (I - W W^H) dW P^{-1}
+  if (dW) {
+    MAK_TRY(G(m, n, n, one_<T>(), opnd<T>(dW, lddw), opnd<T>(Pinv, n), zero_<T>(), Y, m));
+    MAK_TRY(G(n, n, m, one_<T>(), opnd<T>(W, ldw, OP_C), opnd<T>(Y, m), zero_<T>(), Mm, n));
+    MAK_TRY(G(m, n, n, -one_<T>(), opnd<T>(W, ldw), opnd<T>(Mm, n), one_<T>(), Y, m));
+    {
+      dim3 g((unsigned)ceil_div(m, 256), (unsigned)(n < 65535 ? n : 65535));
+      note_launch();
+      add_strided_kernel<T><<<g, 256, 0, st>>>(m, n, Y, m, dA, ldda);
+      MAK_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  note_launch();
+  info_pullback_kernel<T><<<1, 1, 0, st>>>(info, (int)n, it, nullptr, nullptr);
+  MAK_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+constexpr int SIGN_MAXITER = 60;
+
+template <class T>
+static int qr_pullback_entry(int64_t m, int64_t n, int full, void* dAv, int64_t ldda,
+                             const void* Qv, int64_t ldq, const void* Rv, int64_t ldr,
+                             const void* dQv, int64_t lddq, const void* dRv, int64_t lddr,
+                             const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                             mak_info* info, mak_stream_t stream) {
+  const int64_t k = m < n ? m : n;
+  const int64_t qc = full ? m : k, rr = full ? m : k;
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (dAv == nullptr && m * n > 0) return -4;
+  if (ldda < (m > 1 ? m : 1)) return -5;
+  if (Qv == nullptr && m * qc > 0) return -6;
+  if (ldq < (m > 1 ? m : 1)) return -7;
+  if (Rv == nullptr && rr * n > 0) return -8;
+  if (ldr < (rr > 1 ? rr : 1)) return -9;
+  if (dQv && lddq < (m > 1 ? m : 1)) return -11;
+  if (dRv && lddr < (rr > 1 ? rr : 1)) return -13;
+  mak_pullback_opts o{-1.0, -1.0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -14;
+  if (info == nullptr) return -17;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    qr_pullback_run<T>(st, m, n, full, nullptr, ldda, nullptr, ldq, nullptr, ldr, nullptr, lddq,
+                       nullptr, lddr, o.rank_atol, o.gauge_atol, o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -16;
+  }
+  MAK_TRY(info_reset(st, info));
+  Arena ar(work, work_bytes);
+  return qr_pullback_run<T>(st, m, n, full, (T*)dAv, ldda, (const T*)Qv, ldq, (const T*)Rv, ldr,
+                            (const T*)dQv, lddq, (const T*)dRv, lddr, o.rank_atol, o.gauge_atol,
+                            o.precision, ar, info);
+}
+
+template <class T>
+static int polar_pullback_entry(int64_t m, int64_t n, void* dAv, int64_t ldda, const void* Wv,
+                                int64_t ldw, const void* Pv, int64_t ldp, const void* dWv,
+                                int64_t lddw, const void* dPv, int64_t lddp,
+                                const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                mak_info* info, mak_stream_t stream) {
+  if (m < 0) return -1;
+  if (n < 0 || n > m) return -2;
+  if (dAv == nullptr && m * n > 0) return -3;
+  if (ldda < (m > 1 ? m : 1)) return -4;
+  if (Wv == nullptr && m * n > 0) return -5;
+  if (ldw < (m > 1 ? m : 1)) return -6;
+  if (Pv == nullptr && n > 0) return -7;
+  if (ldp < (n > 1 ? n : 1)) return -8;
+  if (dWv && lddw < (m > 1 ? m : 1)) return -10;
+  if (dPv && lddp < (n > 1 ? n : 1)) return -12;
+  mak_pullback_opts o{-1.0, -1.0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -13;
+  if (info == nullptr) return -16;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    polar_pullback_run<T>(st, m, n, nullptr, ldda, nullptr, ldw, nullptr, ldp, nullptr, lddw,
+                          nullptr, lddp, SIGN_MAXITER, o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -15;
+  }
+  MAK_TRY(info_reset(st, info));
+  Arena ar(work, work_bytes);
+  return polar_pullback_run<T>(st, m, n, (T*)dAv, ldda, (const T*)Wv, ldw, (const T*)Pv, ldp,
+                               (const T*)dWv, lddw, (const T*)dPv, lddp, SIGN_MAXITER,
+                               o.precision, ar, info);
+}
+
+template <class T>
+static size_t qr_pb_ws(int64_t m, int64_t n, int full, int prec) {
+  Arena meas(nullptr, 0);
+  qr_pullback_run<T>(0, m, n, full, nullptr, m, nullptr, m, nullptr, m, nullptr, m, nullptr, m,
+                     -1.0, -1.0, prec, meas, nullptr);
+  return meas.off + 256;
+}
+template <class T>
+static size_t polar_pb_ws(int64_t m, int64_t n, int prec) {
+  Arena meas(nullptr, 0);
+  polar_pullback_run<T>(0, m, n, nullptr, m, nullptr, m, nullptr, n, nullptr, m, nullptr, n,
+                        SIGN_MAXITER, prec, meas, nullptr);
+  return meas.off + 256;
+}
+
+}  // namespace mak
+
+using namespace mak;
+
+extern "C" {
+
+int mak_qr_pullback_workspace(int dtype, int64_t m, int64_t n, int full, int precision,
+                              size_t* bytes) {
+  if (bytes == nullptr) return -6;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  switch (dtype) {
+    case MAK_F64: *bytes = qr_pb_ws<double>(m, n, full, precision); break;
+    case MAK_C64: *bytes = qr_pb_ws<zcomplex>(m, n, full, precision); break;
+    case MAK_F32: *bytes = qr_pb_ws<float>(m, n, full, precision); break;
+    case MAK_C32: *bytes = qr_pb_ws<ccomplex>(m, n, full, precision); break;
+    default: return -1;
+  }
+  return 0;
+}
+
+int mak_left_polar_pullback_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                      size_t* bytes) {
+  if (bytes == nullptr) return -5;
+  if (m < 0) return -2;
+  if (n < 0 || n > m) return -3;
+  switch (dtype) {
+    case MAK_F64: *bytes = polar_pb_ws<double>(m, n, precision); break;
+    case MAK_C64: *bytes = polar_pb_ws<zcomplex>(m, n, precision); break;
+    case MAK_F32: *bytes = polar_pb_ws<float>(m, n, precision); break;
+    case MAK_C32: *bytes = polar_pb_ws<ccomplex>(m, n, precision); break;
+    default: return -1;
+  }
+  return 0;
+}
+
+#define MAK_QRPB(NAME, T, PT)                                                                   \
+  int NAME(int64_t m, int64_t n, int full, PT* dA, int64_t ldda, const PT* Q, int64_t ldq,      \
+           const PT* R, int64_t ldr, const PT* dQ, int64_t lddq, const PT* dR, int64_t lddr,    \
+           const mak_pullback_opts* opts, void* work, size_t work_bytes, mak_info* info,        \
+           mak_stream_t stream) {                                                               \
+    return qr_pullback_entry<T>(m, n, full, dA, ldda, Q, ldq, R, ldr, dQ, lddq, dR, lddr, opts, \
+                                work, work_bytes, info, stream);                               \
+  }
+MAK_QRPB(mak_qr_pullback_d, double, double)
+MAK_QRPB(mak_qr_pullback_z, zcomplex, void)
+MAK_QRPB(mak_qr_pullback_s, float, float)
+MAK_QRPB(mak_qr_pullback_c, ccomplex, void)
+
+#define MAK_POLPB(NAME, T, PT)                                                                  \
+  int NAME(int64_t m, int64_t n, PT* dA, int64_t ldda, const PT* W, int64_t ldw, const PT* P,   \
+           int64_t ldp, const PT* dW, int64_t lddw, const PT* dP, int64_t lddp,                 \
+           const mak_pullback_opts* opts, void* work, size_t work_bytes, mak_info* info,        \
+           mak_stream_t stream) {                                                               \
+    return polar_pullback_entry<T>(m, n, dA, ldda, W, ldw, P, ldp, dW, lddw, dP, lddp, opts,    \
+                                   work, work_bytes, info, stream);                            \
+  }
+MAK_POLPB(mak_left_polar_pullback_d, double, double)
+MAK_POLPB(mak_left_polar_pullback_z, zcomplex, void)
+MAK_POLPB(mak_left_polar_pullback_s, float, float)
+MAK_POLPB(mak_left_polar_pullback_c, ccomplex, void)
+
+}  // extern "C"

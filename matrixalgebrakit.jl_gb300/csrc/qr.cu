@@ -261,6 +261,38 @@ __global__ void __launch_bounds__(256) reduce_trmm_kernel(int jb, int nt, int sp
   }
 }
 
+constexpr int QR_OUTER_NB = 128;  // outer block of the mixed-precision path
+
+// T factor (forward, column-wise larft) of a JB-wide block reflector from the
+// Gram matrix G = V^H V (strict upper part used) and tau:
+//   T[0:j, j] = -tau_j T[0:j, 0:j] G[0:j, j],  T[j, j] = tau_j.
+// One CTA; T is kept packed upper-triangular in shared memory.
+template <class T>
+__global__ void __launch_bounds__(128) larft_gram_kernel(int jb, const T* __restrict__ G, int ldg,
+                                                         const T* __restrict__ tau, T* Tout,
+                                                         int ldt) {
+  extern __shared__ __align__(16) unsigned char lg_raw[];
+  T* tp = reinterpret_cast<T*>(lg_raw);  // column j at offset j(j+1)/2
+  __shared__ T tv[QR_OUTER_NB];
+  const int tid = threadIdx.x;
+  for (int j = 0; j < jb; j++) {
+    const T tj = tau[j];
+    if (tid < j) tv[tid] = -(tj * G[tid + (int64_t)j * ldg]);
+    __syncthreads();
+    if (tid < j) {
+      T s = zero_<T>();
+      for (int l = tid; l < j; l++) s = fma_(tp[l * (l + 1) / 2 + tid], tv[l], s);
+      tp[j * (j + 1) / 2 + tid] = s;
+    }
+    if (tid == 0) tp[j * (j + 1) / 2 + j] = tj;
+    __syncthreads();
+  }
+  for (int e = tid; e < jb * jb; e += blockDim.x) {
+    const int i = e % jb, j = e / jb;
+    Tout[i + (int64_t)j * ldt] = (i <= j) ? tp[j * (j + 1) / 2 + i] : zero_<T>();
+  }
+}
+
 template <class T>
 __global__ void signs_kernel(int k, const T* A, int64_t lda, int positive, T* s) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -395,7 +427,6 @@ template <class T>
 int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64_t ldq,
            int64_t qcols, T* R, int64_t ldr, int64_t rrows, int positive, int blocksize,
            int precision, Arena& ar, mak_info* info) {
-  (void)precision;
   const int64_t k = m < n ? m : n;
   const int nb = (blocksize > 0 && blocksize < NBMAX) ? blocksize : NBMAX;
   const int64_t nblk = ceil_div(k, nb);
@@ -403,6 +434,11 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   const int sms = num_sms();
   const int gmax = sms;  // upper bound on panel CTAs (for workspace sizing)
   const int max_splits = 64;
+  // mixed precision: 128-wide outer blocks whose block reflector is applied
+  // with split-precision tensor-core GEMMs (K = 128 or K = m)
+  const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8;
+  const int NBO = mixed ? QR_OUTER_NB : nb;
+  const int64_t nblk_o = ceil_div(k, NBO);
 
   T* tau = ar.take<T>(k > 0 ? k : 1);
   T* Ts = ar.take<T>((size_t)(nblk > 0 ? nblk : 1) * NBMAX * NBMAX);
@@ -414,15 +450,58 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   T* part_g = ar.take<T>((size_t)gmax * NBMAX * NBMAX);
   T* alpha_buf = ar.take<T>(NBMAX);
   unsigned* bar = ar.take<unsigned>(2);
+  T *To = nullptr, *Gm = nullptr, *Wm = nullptr, *W2m = nullptr;
+  char* ozs = nullptr;
+  size_t oz_bytes = 0;
+  if (mixed) {
+    To = ar.take<T>((size_t)(nblk_o > 0 ? nblk_o : 1) * NBO * NBO);
+    Gm = ar.take<T>((size_t)NBO * NBO);
+    Wm = ar.take<T>((size_t)NBO * (wmax > 0 ? wmax : 1));
+    W2m = ar.take<T>((size_t)NBO * (wmax > 0 ? wmax : 1));
+    // the tensor-core GEMMs run one after another and share one scratch region
+    const int64_t shapes[4][3] = {{NBO, wmax, m}, {m, wmax, NBO}, {NBO, wmax, NBO}, {NBO, NBO, m}};
+    for (auto& sh : shapes) {
+      Arena meas(nullptr, 0);
+      gemm_prec<T>(st, precision, sh[0], sh[1], sh[2], one_<T>(), opnd<T>(nullptr, 1),
+                   opnd<T>(nullptr, 1), zero_<T>(), nullptr, 1, meas, nullptr);
+      if (meas.off + 1024 > oz_bytes) oz_bytes = meas.off + 1024;
+    }
+    ozs = ar.take<char>(oz_bytes);
+  }
   if (ar.base == nullptr) return 0;
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
   int* status = &info->status;
 
   MAK_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st));
 
+  // C <- (I - V op(T) V^H) C with the tensor-core GEMMs; op(T) = T^H for the
+  // factorization, T for Q formation (T is JB x JB upper, ld NBO)
+  auto larfb_mixed = [&](const T* V, int64_t mp, int JB, const T* Tm, int conjtrans, T* Cm,
+                         int64_t ldc, int64_t nc) -> int {
+    {
+      Arena oz(ozs, oz_bytes);
+      MAK_TRY(gemm_prec<T>(st, precision, JB, nc, mp, one_<T>(),
+                           opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER), opnd<T>(Cm, ldc), zero_<T>(),
+                           Wm, JB, oz, status));
+    }
+    {
+      Arena oz(ozs, oz_bytes);
+      MAK_TRY(gemm_prec<T>(st, precision, JB, nc, JB, one_<T>(),
+                           opnd<T>(Tm, NBO, conjtrans ? OP_C : OP_N, MASK_UPPER),
+                           opnd<T>(Wm, JB), zero_<T>(), W2m, JB, oz, status));
+    }
+    Arena oz(ozs, oz_bytes);
+    return gemm_prec<T>(st, precision, mp, nc, JB, -one_<T>(),
+                        opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), opnd<T>(W2m, JB), one_<T>(), Cm,
+                        ldc, oz, status);
+  };
+
   // ------------------------------------------------------------ factor
   for (int64_t j0 = 0; j0 < k; j0 += nb) {
     const int jb = (int)((k - j0) < nb ? (k - j0) : nb);
+    const int64_t J0 = (j0 / NBO) * NBO;                       // enclosing outer block
+    const int JB = (int)((k - J0) < NBO ? (k - J0) : NBO);
+    const int64_t col_end = mixed ? J0 + JB : n;              // inner updates stop at the block
     const int64_t mp = m - j0;
     T* Ap = A + j0 + j0 * lda;
     T* Tb = Ts + (j0 / nb) * NBMAX * NBMAX;
@@ -431,11 +510,13 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     PanelArgs<T> pa{Ap, lda, (int)mp, jb, ps.rpc, tau + j0, Tb, part_nrm, part_w,
                     part_g, alpha_buf, bar, status};
     void* args[] = {&pa};
-    ProfScope prof(st, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
-    note_launch();
-    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)qr_panel_kernel<T>, dim3(ps.G),
-                                             dim3(PANEL_THREADS), args, ps.smem, st));
-    const int64_t nt = n - j0 - jb;
+    {
+      ProfScope prof(st, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
+      note_launch();
+      MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)qr_panel_kernel<T>, dim3(ps.G),
+                                               dim3(PANEL_THREADS), args, ps.smem, st));
+    }
+    const int64_t nt = col_end - j0 - jb;
     if (nt > 0) {
       T* C = A + j0 + (j0 + jb) * lda;
       int splits = pick_splits(jb, nt, mp, sms);
@@ -449,6 +530,33 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
       MAK_CUDA_TRY(cudaGetLastError());
       MAK_TRY(gemm<T>(st, mp, nt, jb, -one_<T>(), opnd<T>(Ap, lda, OP_N, MASK_UNIT_LOWER),
                       opnd<T>(W2, jb), one_<T>(), C, lda));
+    }
+    if (mixed && j0 + jb == J0 + JB) {
+      // outer block complete: its T factor from the Gram matrix of V, then
+      // the trailing update with the 128-wide block reflector
+      const T* V = A + J0 + J0 * lda;
+      const int64_t mpo = m - J0;
+      T* Tb_o = To + (J0 / NBO) * NBO * NBO;
+      {
+        Arena oz(ozs, oz_bytes);
+        // the Gram matrix fixes the orthogonality of the block reflector, so
+        // it stays in native FP64 (2 m 128^2 flops per block, split-K)
+        MAK_TRY(gemm_prec<T>(st, MAK_PREC_NATIVE, JB, JB, mpo, one_<T>(),
+                             opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER),
+                             opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), zero_<T>(), Gm, NBO, oz,
+                             status));
+      }
+      static std::once_flag lg_once;
+      std::call_once(lg_once, [] {
+        cudaFuncSetAttribute(larft_gram_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)((size_t)QR_OUTER_NB * (QR_OUTER_NB + 1) / 2 * sizeof(T)));
+      });
+      note_launch();
+      larft_gram_kernel<T><<<1, 128, (size_t)NBO * (NBO + 1) / 2 * sizeof(T), st>>>(
+          JB, Gm, NBO, tau + J0, Tb_o, NBO);
+      MAK_CUDA_TRY(cudaGetLastError());
+      if (J0 + JB < n)
+        MAK_TRY(larfb_mixed(V, mpo, JB, Tb_o, 1, A + J0 + (J0 + JB) * lda, lda, n - J0 - JB));
     }
   }
 
@@ -472,6 +580,17 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   }
 
   // ------------------------------------------- Q = H_1 ... H_k [diag(s); 0]
+  if (mixed) {
+    for (int64_t bo = nblk_o - 1; bo >= 0; bo--) {
+      const int64_t J0 = bo * NBO;
+      const int JB = (int)((k - J0) < NBO ? (k - J0) : NBO);
+      const int64_t qt = qcols - J0;
+      if (qt <= 0) continue;
+      MAK_TRY(larfb_mixed(A + J0 + J0 * lda, m - J0, JB, To + bo * NBO * NBO, 0,
+                          Q + J0 + J0 * ldq, ldq, qt));
+    }
+    return 0;
+  }
   for (int64_t bi = nblk - 1; bi >= 0; bi--) {
     const int64_t j0 = bi * nb;
     const int jb = (int)((k - j0) < nb ? (k - j0) : nb);

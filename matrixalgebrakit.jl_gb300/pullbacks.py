@@ -1,0 +1,119 @@
+"""Reverse rules: ``qr_pullback_`` and ``left_polar_pullback_`` on CUDA tensors.
+
+Mirror ``qr_pullback!(ΔA, A, (Q, R), (ΔQ, ΔR); rank_atol, gauge_atol)``
+(src/pullbacks/qr.jl:73-120) and ``left_polar_pullback!(ΔA, A, (W, P),
+(ΔW, ΔP))`` (src/pullbacks/polar.jl:7-29): ``ΔA`` is accumulated into and
+returned; a cotangent given as ``None`` is a zero tangent
+(``iszerotangent``, src/common/pullbacks.jl:9-12); a gauge-dependent
+cotangent emits the reference's warning (qr.jl:50-51).  These are the
+functions the package's ChainRulesCore and Mooncake rules call
+(ext/MatrixAlgebraKitChainRulesCoreExt.jl:34,254), so the Julia extension
+specialises exactly these two for CuMatrix.
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+import warnings
+
+import torch
+
+from . import _lib
+from .algorithms import ArgumentError, DimensionMismatch
+from .core import (DTYPE_CODE, SUFFIX, check_cuda_tensor, check_rc, check_status, ld_or_raise,
+                   lib, new_info, ptr, read_info, stream_handle, workspace)
+from .qr import PRECISION_CODE
+
+
+def _opts(rank_atol, gauge_atol, precision):
+    return _lib.mak_pullback_opts(-1.0 if rank_atol is None else float(rank_atol),
+                                  -1.0 if gauge_atol is None else float(gauge_atol),
+                                  PRECISION_CODE[precision], 0)
+
+
+def _chk(X, shape, dtype, name):
+    if X is None:
+        return
+    check_cuda_tensor(X, name)
+    if tuple(X.shape) != tuple(shape):
+        raise DimensionMismatch(f"{name} must have size {tuple(shape)}, got {tuple(X.shape)}")
+    if X.dtype != dtype:
+        raise ArgumentError(f"{name} has element type {X.dtype}, expected {dtype}")
+
+
+def qr_pullback_(dA, A, QR, dQR, rank_atol=None, gauge_atol=None, precision="native",
+                 _info=None):
+    """``qr_pullback!``: dA += (pullback of qr_compact / qr_full at (Q, R))."""
+    Q, R = QR
+    dQ, dR = dQR
+    check_cuda_tensor(dA, "dA")
+    m, n = Q.shape[0], R.shape[1]
+    if tuple(dA.shape) != (m, n):
+        raise DimensionMismatch(f"size of dA ({tuple(dA.shape)}) does not match size of Q*R "
+                                f"({m}, {n})")
+    # qr_full and qr_compact only differ when m > n (Q m x m, R m x n)
+    full = int(m > n and Q.shape[1] == m)
+    k = min(m, n)
+    qc = m if full else k
+    _chk(Q, (m, qc), dA.dtype, "Q")
+    _chk(R, (m if full else k, n), dA.dtype, "R")
+    _chk(dQ, Q.shape, dA.dtype, "dQ")
+    _chk(dR, R.shape, dA.dtype, "dR")
+    opts = _opts(rank_atol, gauge_atol, precision)
+    L = lib()
+    nbytes = ct.c_size_t(0)
+    check_rc(L.mak_qr_pullback_workspace(DTYPE_CODE[dA.dtype], m, n, full, opts.precision,
+                                         ct.byref(nbytes)), "mak_qr_pullback_workspace")
+    dev = dA.device
+    with torch.cuda.device(dev):
+        work = workspace(nbytes.value, dev)
+        info = new_info(dev)
+        fn = getattr(L, f"mak_qr_pullback_{SUFFIX[dA.dtype]}")
+        rc = fn(m, n, full, ptr(dA), ld_or_raise(dA, "dA"), ptr(Q), ld_or_raise(Q, "Q"), ptr(R),
+                ld_or_raise(R, "R"), ptr(dQ), ld_or_raise(dQ, "dQ") if dQ is not None else 1,
+                ptr(dR), ld_or_raise(dR, "dR") if dR is not None else 1, ct.byref(opts),
+                ptr(work), nbytes.value, ptr(info), stream_handle(dev))
+        check_rc(rc, fn.__name__)
+        inf = read_info(info)
+    check_status(inf, fn.__name__)
+    if inf.gauge > inf.gauge_atol:
+        warnings.warn(f"`qr` cotangents sensitive to gauge choice: (|Δgauge| = {inf.gauge})",
+                      RuntimeWarning, stacklevel=2)
+    if _info is not None:
+        _info.update(rank=inf.rank, gauge=inf.gauge, gauge_atol=inf.gauge_atol)
+    return dA
+
+
+def left_polar_pullback_(dA, A, WP, dWP, precision="native", _info=None):
+    """``left_polar_pullback!``: dA += (pullback of left_polar at (W, P))."""
+    W, P = WP
+    dW, dP = dWP
+    check_cuda_tensor(dA, "dA")
+    m, n = W.shape
+    if tuple(dA.shape) != (m, n):
+        raise DimensionMismatch(f"dA must have size {(m, n)}")
+    _chk(W, (m, n), dA.dtype, "W")
+    _chk(P, (n, n), dA.dtype, "P")
+    _chk(dW, (m, n), dA.dtype, "dW")
+    _chk(dP, (n, n), dA.dtype, "dP")
+    opts = _opts(None, None, precision)
+    L = lib()
+    nbytes = ct.c_size_t(0)
+    check_rc(L.mak_left_polar_pullback_workspace(DTYPE_CODE[dA.dtype], m, n, opts.precision,
+                                                 ct.byref(nbytes)),
+             "mak_left_polar_pullback_workspace")
+    dev = dA.device
+    with torch.cuda.device(dev):
+        work = workspace(nbytes.value, dev)
+        info = new_info(dev)
+        fn = getattr(L, f"mak_left_polar_pullback_{SUFFIX[dA.dtype]}")
+        rc = fn(m, n, ptr(dA), ld_or_raise(dA, "dA"), ptr(W), ld_or_raise(W, "W"), ptr(P),
+                ld_or_raise(P, "P"), ptr(dW), ld_or_raise(dW, "dW") if dW is not None else 1,
+                ptr(dP), ld_or_raise(dP, "dP") if dP is not None else 1, ct.byref(opts),
+                ptr(work), nbytes.value, ptr(info), stream_handle(dev))
+        check_rc(rc, fn.__name__)
+        inf = read_info(info)
+    check_status(inf, fn.__name__)
+    if _info is not None:
+        _info.update(iterations=inf.iterations)
+    return dA

@@ -110,3 +110,20 @@ def test_left_polar_errors_and_warning(mak, cuda):
     B = to_dev(O.polar_test_matrix(np.random.default_rng(2), 64, np.float64), cuda)
     with pytest.warns(RuntimeWarning, match="did not converge"):
         mak.left_polar(B, maxiter=2)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128], ids=lambda d: np.dtype(d).name)
+@pytest.mark.parametrize("shape", [(300, 300), (700, 260), (512, 512)])
+def test_left_polar_mixed(mak, cuda, dt, shape):
+    """precision="mixed": 128-wide Gauss-Jordan blocks and the Newton/QR
+    products on the split-precision tensor-core GEMM; BASELINE bounds."""
+    rng = np.random.default_rng(25)
+    A = O.polar_test_matrix(rng, shape[0], dt) if shape[0] == shape[1] else O.gaussian(rng, *shape, dt)
+    info = {}
+    W, P = mak.left_polar_(to_dev(A, cuda), None, None, precision="mixed", _info=info)
+    Wh, Ph = to_host(W), to_host(P)
+    assert info["converged"]
+    assert back_err(A, Wh, Ph) <= 1e-12
+    assert O.orth_error(Wh) <= 1e-12 * np.sqrt(shape[1])
+    Wo, Po, _ = O.left_polar_newton(A)
+    assert O.rel_err(Wh, Wo) <= 1e-8 and O.rel_err(Ph, Po) <= 1e-8
