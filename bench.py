@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--no-polar", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--polar-n", type=int, default=8192)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-blocks", type=int, default=300)
     return ap.parse_args()
 
 
@@ -362,7 +364,8 @@ def run_gb300(args):
     tensor_work = g_work.value * (OZ_PAIRS if kind == 1 else 1)
     achieved = tensor_work / (g_ms.value / 1e3) / 1e12 if g_ms.value > 0 else 0.0
     fp64_equiv = g_work.value / (g_ms.value / 1e3) / 1e12 if g_ms.value > 0 else 0.0
-    roofline = {"bound": "tensor", "achieved": round(achieved, 4), "peak": round(peak, 4),
+    roofline = {"bound": "tensor", "achieved": round(achieved, 4),
+                "peak": round(peak, 4) if peak else None,
                 "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
                 "fp64_equivalent_tflops": round(fp64_equiv, 4),
                 "traffic": None,
@@ -426,6 +429,8 @@ def run_gb300(args):
     # left_polar! (Newton) on the single large polar problem
     if not args.no_polar and not args.lean:
         out["polar"] = polar_measure(mak, args, dev)
+    if not args.no_batched and not args.lean:
+        out["batched"] = batched_measure(mak, args, dev)
 
     if rank == 0 and not args.no_cpu_baseline and not args.lean:
         ms_, ns_ = (int(x) for x in args.cpu_sample.split("x"))
@@ -441,6 +446,93 @@ def run_gb300(args):
     if rank == 0:
         print(json.dumps(out), flush=True)
     return 0
+
+
+def batched_measure(mak, args, dev):
+    """Uneven blocks of a block-sparse tensor: m_i ~ U{8..1024}, n_i ~ U{4..m_i},
+    first half Float64, second half ComplexF64 (iid N(0,1), re/im).  qr_compact
+    and left_polar of all blocks in one batched call, captured in a CUDA graph
+    and replayed, against a per-block launch loop of the same factorizations."""
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(SEED + 11)
+    nb = args.batched_blocks
+    shapes = []
+    for i in range(nb):
+        m = int(rng.integers(8, 1025))
+        n = int(rng.integers(4, m + 1))
+        shapes.append((m, n, torch.float64 if i < nb // 2 else torch.complex128))
+
+    def rand(m, n, dt):
+        if dt == torch.complex128:
+            x = rng.standard_normal((n, m)) + 1j * rng.standard_normal((n, m))
+        else:
+            x = rng.standard_normal((n, m))
+        return torch.from_numpy(x).to(dev).t()
+
+    srcs = [rand(m, n, dt) for (m, n, dt) in shapes]
+    work = [s.clone() for s in srcs]
+    flops_qr = sum(qr_flops(m, n, dt == torch.complex128) for (m, n, dt) in shapes)
+    res = {"workload": f"{nb} blocks m~U{{8..1024}} n~U{{4..m}}, half Float64 half ComplexF64",
+           "qr_gflop": round(flops_qr / 1e9, 2)}
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    for prec in ("native", "mixed"):
+        outs = mak.batched_qr_compact(work, copy_inputs=False, precision=prec)
+
+        def restore():
+            for w, s in zip(work, srcs):
+                w.copy_(s)
+
+        # graph capture of the whole batch (inputs restored inside the graph)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            restore()
+            with torch.cuda.graph(g, stream=s):
+                restore()
+                mak.batched_qr_compact(work, copy_inputs=False, outs=outs, precision=prec,
+                                       _capturing=True)
+        torch.cuda.current_stream().wait_stream(s)
+        ms_graph = timed(g.replay)
+
+        def loop():
+            restore()
+            for w, (q, r) in zip(work, outs):
+                mak.qr_compact_(w, (q, r), precision=prec)
+
+        ms_loop = timed(loop, reps=1)
+        res[f"qr_{prec}"] = {"graph_ms": round(ms_graph, 3), "blocks_per_s": round(nb * 1e3 / ms_graph, 1),
+                             "tflops": round(flops_qr / (ms_graph / 1e3) / 1e12, 4),
+                             "per_block_loop_ms": round(ms_loop, 3),
+                             "speedup_vs_loop": round(ms_loop / ms_graph, 2)}
+        del g
+    # polar (batched, fixed Newton iteration count) in both precisions
+    for prec in ("native", "mixed"):
+        def run_polar():
+            for w, s_ in zip(work, srcs):
+                w.copy_(s_)
+            return mak.batched_left_polar(work, copy_inputs=False, precision=prec, maxiter=10)
+
+        outs = run_polar()
+        ms = timed(run_polar, reps=1)
+        back = max(float(torch.linalg.norm(s_ - W @ P) / torch.linalg.norm(s_))
+                   for s_, (W, P) in zip(srcs[:8] + srcs[-8:], outs[:8] + outs[-8:]))
+        res[f"polar_{prec}"] = {"ms": round(ms, 3), "blocks_per_s": round(nb * 1e3 / ms, 1),
+                                "newton_iterations": 10, "max_back_err_sampled": back}
+    return res
 
 
 def polar_measure(mak, args, dev):

@@ -77,7 +77,10 @@ typedef struct {
 typedef struct {
   int32_t maxiter;   /* reference default 10                                  */
   int32_t precision; /* MAK_PREC_NATIVE or MAK_PREC_MIXED                     */
-  double tol;        /* <= 0: reference default eps(real T)^(2/3)             */
+  double tol;        /* > 0: stopping tolerance; 0: reference default
+                        eps(real T)^(2/3); < 0: run exactly maxiter iterations
+                        with no host synchronization (CUDA-graph capturable;
+                        `converged` is reported against the default tol)    */
 } mak_polar_opts;
 
 /* Options of the pullbacks (reference src/pullbacks/qr.jl:73-77). */
@@ -187,6 +190,38 @@ int mak_left_polar_newton_s(int64_t m, int64_t n, float* A, int64_t lda, float* 
 int mak_left_polar_newton_c(int64_t m, int64_t n, void* A, int64_t lda, void* W, int64_t ldw,
                             void* P, int64_t ldp, const mak_polar_opts* opts, void* work,
                             size_t work_bytes, mak_info* info, mak_stream_t stream);
+
+/* -------------------------------------------------------------- batched ---
+ * Many independent, uneven blocks in one stream-ordered call (the symmetry
+ * sectors of a block-sparse tensor).  The reference has no batched entry: a
+ * caller loops qr_compact! / left_polar! over the blocks.  Items live in HOST
+ * memory and hold DEVICE pointers; element types may be mixed.  Blocks are
+ * scheduled longest-first over internal streams that fork from and join back
+ * into `stream`, so the whole batch can be captured into a CUDA graph (the
+ * internal streams are created by the first call, which must precede any
+ * capture).  `infos` is a DEVICE array of nitems records.  Batched polar runs
+ * exactly opts->maxiter Newton iterations (no host synchronization).
+ */
+typedef struct {
+  int32_t dtype;    /* MAK_F64 / MAK_C64 / MAK_F32 / MAK_C32                 */
+  int32_t reserved;
+  int64_t m, n;
+  void* A;          /* m x n, destroyed                                      */
+  int64_t lda;
+  void* Q;          /* QR: Q (m x min(m,n));  polar: W (m x n)               */
+  int64_t ldq;
+  void* R;          /* QR: R (min(m,n) x n);  polar: P (n x n); NULL = skip  */
+  int64_t ldr;
+} mak_batch_item;
+
+int mak_batched_qr_workspace(const mak_batch_item* items, int nitems, const mak_qr_opts* opts,
+                             size_t* bytes);
+int mak_batched_qr_compact(const mak_batch_item* items, int nitems, const mak_qr_opts* opts,
+                           void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream);
+int mak_batched_left_polar_workspace(const mak_batch_item* items, int nitems,
+                                     const mak_polar_opts* opts, size_t* bytes);
+int mak_batched_left_polar(const mak_batch_item* items, int nitems, const mak_polar_opts* opts,
+                           void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream);
 
 /* ------------------------------------------------------------ pullbacks ---
  * qr_pullback!(dA, A, (Q, R), (dQ, dR); rank_atol, gauge_atol)

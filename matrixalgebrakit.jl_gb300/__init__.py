@@ -41,3 +41,7 @@ def library():
 from .pullbacks import left_polar_pullback_, qr_pullback_  # noqa: E402
 
 __all__ += ["qr_pullback_", "left_polar_pullback_"]
+
+from .batched import batched_left_polar, batched_qr_compact  # noqa: E402
+
+__all__ += ["batched_qr_compact", "batched_left_polar"]

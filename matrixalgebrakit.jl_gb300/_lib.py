@@ -115,3 +115,20 @@ def load():
 
 def status_string(code: int) -> str:
     return load().mak_status_string(code).decode()
+
+
+class mak_batch_item(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("reserved", C.c_int32), ("m", C.c_int64),
+                ("n", C.c_int64), ("A", C.c_void_p), ("lda", C.c_int64), ("Q", C.c_void_p),
+                ("ldq", C.c_int64), ("R", C.c_void_p), ("ldr", C.c_int64)]
+
+
+SIGNATURES["mak_batched_qr_workspace"] = (C.c_int, [C.POINTER(mak_batch_item), C.c_int,
+                                                    C.POINTER(mak_qr_opts), C.POINTER(_sz)])
+SIGNATURES["mak_batched_qr_compact"] = (C.c_int, [C.POINTER(mak_batch_item), C.c_int,
+                                                  C.POINTER(mak_qr_opts), _p, _sz, _p, _p])
+SIGNATURES["mak_batched_left_polar_workspace"] = (C.c_int, [C.POINTER(mak_batch_item), C.c_int,
+                                                            C.POINTER(mak_polar_opts),
+                                                            C.POINTER(_sz)])
+SIGNATURES["mak_batched_left_polar"] = (C.c_int, [C.POINTER(mak_batch_item), C.c_int,
+                                                  C.POINTER(mak_polar_opts), _p, _sz, _p, _p])

@@ -1,0 +1,213 @@
+// Batched QR / polar over a list of independent, uneven blocks (the symmetry
+// sectors of a block-sparse tensor), GB300 native.
+//
+// The reference has no batched API: a caller loops over blocks and calls
+// qr_compact! / left_polar! once per block (SURVEY: C3 / C5 workloads).  Here
+// one call takes the whole work list:
+//  * blocks are ordered by estimated flops (longest first) and dealt to the
+//    least-loaded of BATCH_STREAMS internal streams (LPT schedule), so large
+//    blocks keep their multi-CTA kernels while small blocks fill the
+//    remaining SMs concurrently;
+//  * the internal streams fork from and join back into the caller's stream
+//    with events, so the whole batch is one stream-ordered unit that a
+//    caller can capture into a CUDA graph (the streams and events are
+//    created on the first call, which must therefore precede any capture);
+//  * each stream owns a slice of the caller's workspace sized for the
+//    largest block it runs; every block writes its own mak_info record;
+//  * batched polar runs the Newton iteration in its fixed-iteration mode
+//    (maxiter iterations, no host synchronization).
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "internal.h"
+
+namespace mak {
+
+constexpr int BATCH_STREAMS = 8;
+
+struct StreamPool {
+  cudaStream_t s[BATCH_STREAMS];
+  cudaEvent_t fork, join[BATCH_STREAMS];
+  bool ok = false;
+};
+
+static StreamPool& pool() {
+  static StreamPool p;
+  static std::once_flag f;
+  std::call_once(f, [] {
+    bool ok = true;
+    for (int i = 0; i < BATCH_STREAMS; i++) {
+      ok &= cudaStreamCreateWithFlags(&p.s[i], cudaStreamNonBlocking) == cudaSuccess;
+      ok &= cudaEventCreateWithFlags(&p.join[i], cudaEventDisableTiming) == cudaSuccess;
+    }
+    ok &= cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming) == cudaSuccess;
+    p.ok = ok;
+  });
+  return p;
+}
+
+enum { BATCH_QR = 0, BATCH_POLAR = 1 };
+
+template <class T>
+static int item_run(int kind, const mak_batch_item& it, const void* opts, Arena& ar,
+                    mak_info* info, cudaStream_t st) {
+  const int64_t m = it.m, n = it.n;
+  if (kind == BATCH_QR) {
+    const mak_qr_opts* o = (const mak_qr_opts*)opts;
+    const int64_t k = m < n ? m : n;
+    return qr_run<T>(st, m, n, (T*)it.A, it.lda, (T*)it.Q, it.ldq, k, (T*)it.R, it.ldr, k,
+                     o->positive, o->blocksize, o->precision, ar, info);
+  }
+  const mak_polar_opts* o = (const mak_polar_opts*)opts;
+  // fixed-iteration mode (negative tol); default tol = eps(real T)^(2/3)
+  const double dtol = sizeof(real_t<T>) == 8 ? 3.6700562101601e-11 : 2.4214387e-5;
+  const double tol = -(o->tol > 0 ? o->tol : dtol);
+  return polar_newton_run<T>(st, m, n, (T*)it.A, it.lda, (T*)it.Q, it.ldq, (T*)it.R, it.ldr,
+                             o->maxiter, tol, o->precision, ar, info);
+}
+
+static int item_dispatch(int kind, const mak_batch_item& it, const void* opts, Arena& ar,
+                         mak_info* info, cudaStream_t st) {
+  switch (it.dtype) {
+    case MAK_F64: return item_run<double>(kind, it, opts, ar, info, st);
+    case MAK_C64: return item_run<zcomplex>(kind, it, opts, ar, info, st);
+    case MAK_F32: return item_run<float>(kind, it, opts, ar, info, st);
+    case MAK_C32: return item_run<ccomplex>(kind, it, opts, ar, info, st);
+    default: return MAK_ERR_UNSUPPORTED;
+  }
+}
+
+static double item_flops(int kind, const mak_batch_item& it) {
+  const double m = (double)it.m, n = (double)it.n;
+  const double c = (it.dtype == MAK_C64 || it.dtype == MAK_C32) ? 4.0 : 1.0;
+  const double k = m < n ? m : n;
+  double f = c * (4.0 * m * k * k - 4.0 * k * k * k / 3.0);
+  if (kind == BATCH_POLAR) f += c * 10.0 * 2.0 * n * n * n;
+  return f + 1e6;  // launch overheads dominate tiny blocks
+}
+
+struct Plan {
+  std::vector<int> owner;            // stream of each item
+  std::vector<size_t> ws_item;       // workspace of each item
+  size_t ws_stream[BATCH_STREAMS];   // slice size per stream
+  size_t off[BATCH_STREAMS];
+  size_t total;
+};
+
+static int plan(int kind, const mak_batch_item* items, int nitems, const void* opts, Plan& p) {
+  p.owner.assign(nitems, 0);
+  p.ws_item.assign(nitems, 0);
+  std::vector<int> order(nitems);
+  for (int i = 0; i < nitems; i++) {
+    order[i] = i;
+    Arena meas(nullptr, 0);
+    mak_batch_item probe = items[i];
+    probe.A = probe.Q = probe.R = nullptr;
+    if (kind == BATCH_POLAR && items[i].R != nullptr) probe.R = (void*)16;  // P wanted
+    int rc = item_dispatch(kind, probe, opts, meas, nullptr, 0);
+    if (rc != 0) return rc;
+    p.ws_item[i] = meas.off + 512;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return item_flops(kind, items[a]) > item_flops(kind, items[b]);
+  });
+  double load[BATCH_STREAMS] = {0};
+  for (int s = 0; s < BATCH_STREAMS; s++) p.ws_stream[s] = 0;
+  for (int i : order) {
+    int best = 0;
+    for (int s = 1; s < BATCH_STREAMS; s++)
+      if (load[s] < load[best]) best = s;
+    p.owner[i] = best;
+    load[best] += item_flops(kind, items[i]);
+    if (p.ws_item[i] > p.ws_stream[best]) p.ws_stream[best] = p.ws_item[i];
+  }
+  p.total = 0;
+  for (int s = 0; s < BATCH_STREAMS; s++) {
+    p.off[s] = p.total;
+    p.total += align_up(p.ws_stream[s], 256);
+  }
+  return 0;
+}
+
+static int batched(int kind, const mak_batch_item* items, int nitems, const void* opts,
+                   void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream) {
+  if (items == nullptr && nitems > 0) return -1;
+  if (nitems < 0) return -2;
+  for (int i = 0; i < nitems; i++) {
+    const mak_batch_item& it = items[i];
+    if (it.m < 0 || it.n < 0 || it.lda < (it.m > 1 ? it.m : 1) || it.ldq < (it.m > 1 ? it.m : 1))
+      return -1;
+    if (kind == BATCH_POLAR && it.n > it.m) return -1;
+    if (it.dtype < MAK_F64 || it.dtype > MAK_C32) return -1;
+  }
+  if (opts == nullptr) return -3;
+  Plan p;
+  MAK_TRY(plan(kind, items, nitems, opts, p));
+  if (work == nullptr && p.total > 0) return -4;
+  if (p.total > work_bytes) return -5;
+  if (infos == nullptr && nitems > 0) return -6;
+  if (nitems == 0) return 0;
+  StreamPool& sp = pool();
+  if (!sp.ok) return MAK_ERR_CUDA;
+  cudaStream_t st = (cudaStream_t)stream;
+  MAK_CUDA_TRY(cudaEventRecord(sp.fork, st));
+  for (int s = 0; s < BATCH_STREAMS; s++) MAK_CUDA_TRY(cudaStreamWaitEvent(sp.s[s], sp.fork, 0));
+  // issue in schedule order so that each stream starts with its largest block
+  std::vector<int> order(nitems);
+  for (int i = 0; i < nitems; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return item_flops(kind, items[a]) > item_flops(kind, items[b]);
+  });
+  int rc_all = 0;
+  set_lookahead(false);  // the batch's streams already overlap the blocks
+  for (int i : order) {
+    const int s = p.owner[i];
+    Arena ar((char*)work + p.off[s], p.ws_stream[s]);
+    int rc = info_reset(sp.s[s], infos + i);
+    if (rc == 0) rc = item_dispatch(kind, items[i], opts, ar, infos + i, sp.s[s]);
+    if (rc != 0 && rc_all == 0) rc_all = rc;
+  }
+  set_lookahead(true);
+  for (int s = 0; s < BATCH_STREAMS; s++) {
+    MAK_CUDA_TRY(cudaEventRecord(sp.join[s], sp.s[s]));
+    MAK_CUDA_TRY(cudaStreamWaitEvent(st, sp.join[s], 0));
+  }
+  return rc_all;
+}
+
+static int batched_ws(int kind, const mak_batch_item* items, int nitems, const void* opts,
+                      size_t* bytes) {
+  if (bytes == nullptr) return -4;
+  if (items == nullptr && nitems > 0) return -1;
+  if (opts == nullptr) return -3;
+  Plan p;
+  MAK_TRY(plan(kind, items, nitems, opts, p));
+  *bytes = p.total + 256;
+  return 0;
+}
+
+}  // namespace mak
+
+using namespace mak;
+
+extern "C" {
+
+int mak_batched_qr_workspace(const mak_batch_item* items, int nitems, const mak_qr_opts* opts,
+                             size_t* bytes) {
+  return batched_ws(BATCH_QR, items, nitems, opts, bytes);
+}
+int mak_batched_qr_compact(const mak_batch_item* items, int nitems, const mak_qr_opts* opts,
+                           void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream) {
+  return batched(BATCH_QR, items, nitems, opts, work, work_bytes, infos, stream);
+}
+int mak_batched_left_polar_workspace(const mak_batch_item* items, int nitems,
+                                     const mak_polar_opts* opts, size_t* bytes) {
+  return batched_ws(BATCH_POLAR, items, nitems, opts, bytes);
+}
+int mak_batched_left_polar(const mak_batch_item* items, int nitems, const mak_polar_opts* opts,
+                           void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream) {
+  return batched(BATCH_POLAR, items, nitems, opts, work, work_bytes, infos, stream);
+}
+
+}  // extern "C"

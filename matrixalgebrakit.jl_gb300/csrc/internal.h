@@ -24,6 +24,17 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
 
 int info_reset(cudaStream_t st, mak_info* info);
 
+// QR look-ahead (side stream) on/off for calls made from the current thread
+bool lookahead_enabled();
+void set_lookahead(bool on);
+
+// Left polar decomposition by scaled Newton (W m x n, P n x n or nullptr);
+// tol < 0 selects the fixed-iteration, host-sync-free mode.
+template <class T>
+int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* W, int64_t ldw,
+                     T* P, int64_t ldp, int maxiter, double tol, int precision, Arena& ar,
+                     mak_info* info);
+
 }  // namespace mak
 
 #include "gemm.cuh"

@@ -154,6 +154,15 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// x * 2^e by integer arithmetic on the exponent field (ldexp outside the
+// normal range)
+__device__ __forceinline__ double scale_pow2(double x, int e) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0 || ex + e <= 0 || ex + e >= 2047) return ldexp(x, e);
+  return __longlong_as_double(b + ((long long)e << 52));
+}
+
 // group accumulator of pair (p, q) (1-based digits): 0..4 exact groups d=2..6; 5 tail
 constexpr int OZ_EXACT = 6;                // exact groups d = 2 .. OZ_EXACT + 1
 constexpr int OZ_NGROUPS = OZ_EXACT + 1;   // + the tail
@@ -319,9 +328,15 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       mbar_arrive(&acc_empty);
     }
     if (ok) {
-      // final: value = 2^(E+F-12) (acc 2^(-6(OZ_EXACT-1)) + tail)
+      // final: value = 2^(E+F-12-SH) (acc + tail 2^SH), SH = 6(OZ_EXACT-1).
+      // The FP64 pipe is 1/1900 of the tensor rate, so each output costs two
+      // conversions and two FP64 FMAs; the scale alpha 2^e is built by
+      // integer exponent arithmetic.
+      constexpr int SH = OZ_BITS * (OZ_EXACT - 1);
       const int gi = m0 + r;
       const int Ei = (gi < a.M) ? a.EA[gi] : 0;
+      const double mult = a.part ? 1.0 : a.alpha;
+      const bool beta0 = a.part != nullptr || a.beta == 0.0, beta1 = a.beta == 1.0;
 #pragma unroll
       for (int c0 = 0; c0 < OZ_BN; c0 += 16) {
         float tl[16];
@@ -331,12 +346,11 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         for (int j = 0; j < 16; j++) {
           const int gj = n0 + c0 + j;
           if (gi >= a.M || gj >= a.Nl) continue;
-          const int e = Ei + a.EB[gj];
-          const double v =
-              ldexp((double)acc[c0 + j], e - 2 * OZ_BITS - OZ_BITS * (OZ_EXACT - 1)) +
-              ldexp((double)tl[j], e - 2 * OZ_BITS);
+          // the tail carries bits below the 2^-SH unit of acc: add it in FP64
+          const double v = fma((double)tl[j], (double)(1ll << SH), (double)acc[c0 + j]);
+          const double sc = scale_pow2(mult, Ei + a.EB[gj] - 2 * OZ_BITS - SH);
           if (a.part) {
-            a.part[(int64_t)gj * a.M + gi] = v;  // split-K partial, ld = M
+            a.part[(int64_t)gj * a.M + gi] = v * sc;  // split-K partial, ld = M
             continue;
           }
           double* dst;
@@ -346,9 +360,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           } else {
             dst = a.C + (int64_t)gi + (int64_t)gj * a.ldc;
           }
-          double out = a.alpha * v;
-          if (a.beta != 0.0) out = fma(a.beta, *dst, out);
-          *dst = out;
+          *dst = beta0 ? v * sc : (beta1 ? fma(v, sc, *dst) : fma(v, sc, a.beta * *dst));
         }
       }
     }
@@ -429,26 +441,33 @@ __device__ __forceinline__ int exp_of_absbits(unsigned long long b) {
   return ex - 1022;
 }
 
-// E[r] for r < R (logical rows)
+// Row maxima of |X| as IEEE bit patterns (non-negative doubles order like
+// their bits), accumulated with atomicMax over a 2-D grid of (rows, K
+// chunks) so that tall K ranges are read by many CTAs in parallel.
+constexpr int OZ_EXP_KCHUNK = 1024;
 template <class T>
-__global__ void oz_exp_kernel(OzSrc<T> s, int R, int K, int* E) {
+__global__ void __launch_bounds__(256) oz_absmax_kernel(OzSrc<T> s, int R, int K,
+                                                        unsigned long long* mx_bits) {
+  const int k0 = blockIdx.y * OZ_EXP_KCHUNK;
+  const int k1 = min(K, k0 + OZ_EXP_KCHUNK);
   if (oz_contig_r(s)) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    // 256 consecutive rows per CTA, each thread walks the chunk of K
+    const int r = blockIdx.x * 256 + threadIdx.x;
     if (r >= R) return;
     unsigned long long mx = 0;
-    for (int k = 0; k < K; k++) {
-      unsigned long long b = absbits(oz_fetch(s, r, k));
+    for (int k = k0; k < k1; k++) {
+      const unsigned long long b = absbits(oz_fetch(s, r, k));
       mx = b > mx ? b : mx;
     }
-    E[r] = exp_of_absbits(mx);
+    if (mx) atomicMax(&mx_bits[r], mx);
   } else {
-    const int warps = blockDim.x >> 5;
-    const int r = blockIdx.x * warps + (threadIdx.x >> 5);
+    // 8 rows per CTA, one warp per row, lanes along K
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (r >= R) return;
     unsigned long long mx = 0;
-    for (int k = lane; k < K; k += 32) {
-      unsigned long long b = absbits(oz_fetch(s, r, k));
+    for (int k = k0 + lane; k < k1; k += 32) {
+      const unsigned long long b = absbits(oz_fetch(s, r, k));
       mx = b > mx ? b : mx;
     }
 #pragma unroll
@@ -456,8 +475,24 @@ __global__ void oz_exp_kernel(OzSrc<T> s, int R, int K, int* E) {
       unsigned long long o = __shfl_xor_sync(0xffffffffu, mx, m);
       mx = o > mx ? o : mx;
     }
-    if (lane == 0) E[r] = exp_of_absbits(mx);
+    if (lane == 0 && mx) atomicMax(&mx_bits[r], mx);
   }
+}
+__global__ void oz_exp_from_bits_kernel(int R, const unsigned long long* mx_bits, int* E) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < R) E[r] = exp_of_absbits(mx_bits[r]);
+}
+template <class T>
+static int oz_exponents(cudaStream_t st, const OzSrc<T>& s, int R, int K, unsigned long long* bits,
+                        int* E) {
+  MAK_CUDA_TRY(cudaMemsetAsync(bits, 0, (size_t)R * sizeof(unsigned long long), st));
+  const unsigned gy = (unsigned)ceil_div(K > 0 ? K : 1, OZ_EXP_KCHUNK);
+  const unsigned gx = (unsigned)(oz_contig_r(s) ? ceil_div(R, 256) : ceil_div(R, 8));
+  note_launch();
+  oz_absmax_kernel<T><<<dim3(gx, gy), 256, 0, st>>>(s, R, K, bits);
+  note_launch();
+  oz_exp_from_bits_kernel<<<(unsigned)ceil_div(R, 256), 256, 0, st>>>(R, bits, E);
+  return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
 
 // planes[p][r][k] (Rpad x Kpad, bf16) = sign * digit_p * 2^(-7(p-1)), zero padded
@@ -598,6 +633,8 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
 
   int* EA = ar.take<int>(Mpad);
   int* EB = ar.take<int>(Npad);
+  unsigned long long* bitsA = ar.take<unsigned long long>(Mpad);
+  unsigned long long* bitsB = ar.take<unsigned long long>(Npad);
   __nv_bfloat16* PA = ar.take<__nv_bfloat16>((size_t)S * Mpad * Kpad);
   __nv_bfloat16* PB = ar.take<__nv_bfloat16>((size_t)S * Npad * Kpad);
   double* part = splits > 1 ? ar.take<double>((size_t)splits * M * Nl) : nullptr;
@@ -607,16 +644,8 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
 
   OzSrc<T> sa{A, 0, (int)M, (int)K};
   OzSrc<T> sb{B, 1, (int)N, (int)K};
-  note_launch();
-  if (oz_contig_r(sa))
-    oz_exp_kernel<T><<<(unsigned)ceil_div(M, 128), 128, 0, st>>>(sa, (int)M, (int)Kl, EA);
-  else
-    oz_exp_kernel<T><<<(unsigned)ceil_div(M, 8), 256, 0, st>>>(sa, (int)M, (int)Kl, EA);
-  note_launch();
-  if (oz_contig_r(sb))
-    oz_exp_kernel<T><<<(unsigned)ceil_div(Nl, 128), 128, 0, st>>>(sb, (int)Nl, (int)Kl, EB);
-  else
-    oz_exp_kernel<T><<<(unsigned)ceil_div(Nl, 8), 256, 0, st>>>(sb, (int)Nl, (int)Kl, EB);
+  MAK_TRY(oz_exponents<T>(st, sa, (int)M, (int)Kl, bitsA, EA));
+  MAK_TRY(oz_exponents<T>(st, sb, (int)Nl, (int)Kl, bitsB, EB));
   note_launch();
   oz_split_kernel<T, S><<<dim3((unsigned)(Kpad / 64 + (Kpad % 64 ? 1 : 0)), (unsigned)(Mpad / 64)),
                           256, 0, st>>>(sa, (int)M, (int)Kl, (int)Mpad, (int)Kpad, EA, PA);

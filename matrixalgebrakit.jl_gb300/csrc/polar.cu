@@ -357,6 +357,14 @@ __global__ void __launch_bounds__(256) newton_update_kernel(int n, T* X, int64_t
 }
 
 template <class T>
+__global__ void info_polar_dev_kernel(mak_info* info, int it, const real_t<T>* conv,
+                                      real_t<T> tol) {
+  info->iterations = it;
+  info->residual = (double)*conv;
+  info->converged = (*conv <= tol) ? 1 : 0;
+}
+
+template <class T>
 __global__ void info_polar_kernel(mak_info* info, int it, double conv, int converged) {
   info->iterations = it;
   info->residual = conv;
@@ -389,8 +397,18 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
     Arena meas(nullptr, 0);
     gje_inverse<T>(st, n, nullptr, n, nullptr, precision, meas, nullptr);
     gj_ws = meas.off + 256;
+    for (int64_t mm : {m, n}) {  // W = Q X and P = X^H R products
+      Arena m2(nullptr, 0);
+      gemm_prec<T>(st, precision, mm, n, n, one_<T>(), opnd<T>(nullptr, 1), opnd<T>(nullptr, 1),
+                   zero_<T>(), nullptr, 1, m2, nullptr);
+      if (m2.off + 256 > gj_ws) gj_ws = m2.off + 256;
+    }
   }
   const size_t tail_bytes = qr_ws > gj_ws ? qr_ws : gj_ws;
+  // tol < 0: run exactly maxiter iterations with no host synchronization
+  // (graph-capturable; |tol| still decides the reported convergence flag)
+  const bool fixed_iters = tol < 0;
+  if (fixed_iters) tol = -tol;
   char* tail = ar.take<char>(tail_bytes);
   if (ar.base == nullptr) return 0;
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
@@ -421,30 +439,39 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
     note_launch();
     newton_update_kernel<T><<<g, 256, 0, st>>>((int)n, X, n, Y, n, iperm, nrm2, conv);
     MAK_CUDA_TRY(cudaGetLastError());
-    MAK_CUDA_TRY(cudaMemcpyAsync(&hconv, conv, sizeof(R), cudaMemcpyDeviceToHost, st));
-    MAK_CUDA_TRY(cudaStreamSynchronize(st));
-    if (!(hconv > (R)tol)) {  // also stops on NaN
-      converged = hconv <= (R)tol;
-      break;
+    if (!fixed_iters) {
+      MAK_CUDA_TRY(cudaMemcpyAsync(&hconv, conv, sizeof(R), cudaMemcpyDeviceToHost, st));
+      MAK_CUDA_TRY(cudaStreamSynchronize(st));
+      if (!(hconv > (R)tol)) {  // also stops on NaN
+        converged = hconv <= (R)tol;
+        break;
+      }
     }
   }
   if (it > maxiter) it = maxiter;
   note_launch();
-  info_polar_kernel<T><<<1, 1, 0, st>>>(info, n > 0 ? it : 0, (double)hconv, converged ? 1 : 0);
+  if (fixed_iters)
+    info_polar_dev_kernel<T><<<1, 1, 0, st>>>(info, n > 0 ? maxiter : 0, conv, (R)tol);
+  else
+    info_polar_kernel<T><<<1, 1, 0, st>>>(info, n > 0 ? it : 0, (double)hconv, converged ? 1 : 0);
   MAK_CUDA_TRY(cudaGetLastError());
 
+  auto G = [&](int64_t M_, int64_t N_, int64_t K_, Operand<T> a, Operand<T> b, T* C_,
+               int64_t ldc) -> int {
+    Arena oz(tail, tail_bytes);
+    return gemm_prec<T>(st, precision, M_, N_, K_, one_<T>(), a, b, zero_<T>(), C_, ldc, oz,
+                        &info->status);
+  };
   if (m > n) {
-    MAK_TRY(gemm<T>(st, m, n, n, one_<T>(), opnd<T>(Qw, m), opnd<T>(X, n), zero_<T>(), W, ldw));
+    MAK_TRY(G(m, n, n, opnd<T>(Qw, m), opnd<T>(X, n), W, ldw));
     if (want_p) {
-      MAK_TRY(gemm<T>(st, n, n, n, one_<T>(), opnd<T>(X, n, OP_C), opnd<T>(Rw, n, OP_N, MASK_UPPER),
-                      zero_<T>(), P, ldp));
+      MAK_TRY(G(n, n, n, opnd<T>(X, n, OP_C), opnd<T>(Rw, n, OP_N, MASK_UPPER), P, ldp));
       MAK_TRY(herm_project<T>(st, n, P, ldp));
     }
   } else {
     MAK_TRY(copy_mat<T>(st, n, n, X, n, W, ldw));
     if (want_p) {
-      MAK_TRY(gemm<T>(st, n, n, n, one_<T>(), opnd<T>(X, n, OP_C), opnd<T>(A0, n), zero_<T>(), P,
-                      ldp));
+      MAK_TRY(G(n, n, n, opnd<T>(X, n, OP_C), opnd<T>(A0, n), P, ldp));
       MAK_TRY(herm_project<T>(st, n, P, ldp));
     }
   }
@@ -486,7 +513,9 @@ static int polar_entry(int64_t m, int64_t n, void* Av, int64_t lda, void* Wv, in
   if (opts) o = *opts;
   if (o.maxiter < 1) return -9;
   if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -9;
-  const double tol = o.tol > 0 ? o.tol : default_tol<T>();
+  // tol < 0 selects the fixed-iteration (no host sync) mode, reported
+  // against the default tolerance
+  const double tol = o.tol > 0 ? o.tol : (o.tol < 0 ? -default_tol<T>() : default_tol<T>());
   if (info == nullptr) return -12;
   cudaStream_t st = (cudaStream_t)stream;
   {

@@ -50,7 +50,46 @@ struct PanelArgs {
   T* alpha_buf;         // [NBMAX]
   unsigned* bar;        // grid barrier words
   int* status;
+  int gstride;          // allocation stride of the per-CTA partial rows
 };
+
+// (scale, ssq) accumulation: the represented value is scale^2 * ssq
+template <class R>
+__device__ __forceinline__ void ssq_merge(R& s, R& q, R s2, R q2) {
+  if (s2 == R(0)) return;
+  if (s < s2) {
+    const R t = s / s2;
+    q = q2 + q * t * t;
+    s = s2;
+  } else {
+    const R t = s2 / s;
+    q += q2 * t * t;
+  }
+}
+template <class R> __device__ __forceinline__ void ssq_add(R& s, R& q, R x) {
+  ssq_merge(s, q, fabs(x), x != R(0) ? R(1) : R(0));
+}
+template <class R> __device__ __forceinline__ void ssq_add(R& s, R& q, cplx<R> x) {
+  ssq_add(s, q, x.re);
+  ssq_add(s, q, x.im);
+}
+// block-wide (scale, ssq) combine, result in every thread (fixed order)
+template <class R, class T>
+__device__ __forceinline__ void ssq_block(R& s, R& q, R* sh_s, T* sh_q_raw) {
+  R* sh_q = reinterpret_cast<R*>(sh_q_raw);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    R s2 = __shfl_xor_sync(0xffffffffu, s, o), q2 = __shfl_xor_sync(0xffffffffu, q, o);
+    ssq_merge(s, q, s2, q2);
+  }
+  __syncthreads();
+  if (lane == 0) { sh_s[wid] = s; sh_q[wid] = q; }
+  __syncthreads();
+  s = R(0);
+  q = R(0);
+  for (int w = 0; w < nw; w++) ssq_merge(s, q, sh_s[w], sh_q[w]);
+}
 
 // beta / tau / 1/(alpha-beta) of one reflector, LAPACK ?larfg convention:
 // H^H [alpha; x] = [beta; 0], H = I - tau v v^H, v = [1; x/(alpha-beta)].
@@ -93,40 +132,29 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
 
   for (int j = 0; j < jb; j++) {
     T* col = Ps + j * rpc;
-    // ---- phase A: scaled sum of squares of x = column j below the diagonal
+    // ---- phase A: one-pass scaled sum of squares (scale, ssq) of x = column
+    // j below the diagonal (LAPACK lassq-style update, overflow safe)
     const int rs = max(0, j + 1 - r0);
-    R mx = R(0);
-    for (int r = rs + tid; r < nr; r += blockDim.x) mx = fmax(mx, abs_(col[r]));
-    mx = block_max(mx, red_r);
-    R ssq = R(0);
-    if (mx > R(0)) {
-      R inv = R(1) / mx;
-      for (int r = rs + tid; r < nr; r += blockDim.x) ssq += abs2_(col[r] * inv);
-    }
-    ssq = block_sum(ssq, red_r);
+    R scl = R(0), ssq = R(0);
+    for (int r = rs + tid; r < nr; r += blockDim.x) ssq_add(scl, ssq, col[r]);
+    ssq_block(scl, ssq, red_r, red_t);
     if (tid == 0) {
-      a.part_nrm[2 * b] = mx;
-      a.part_nrm[2 * b + 1] = ssq;
+      a.part_nrm[b] = scl;
+      a.part_nrm[a.gstride + b] = ssq;
       if (j >= r0 && j < r0 + nr) a.alpha_buf[j] = col[j - r0];
     }
     if (!grid_barrier(a.bar, G, a.status)) return;
 
     // ---- phase B: every CTA derives the same beta/tau from the partials
     if (wid == 0) {
-      R m = R(0);
-      for (int q = lane; q < G; q += 32) m = fmax(m, ld_cg(&a.part_nrm[2 * q]));
-      m = warp_max(m);
-      R s = R(0);
-      if (m > R(0)) {
-        for (int q = lane; q < G; q += 32) {
-          R sq = ld_cg(&a.part_nrm[2 * q]);
-          if (sq > R(0)) {
-            R t = sq / m;
-            s += ld_cg(&a.part_nrm[2 * q + 1]) * t * t;
-          }
-        }
+      R m = R(0), s = R(0);
+      for (int q = lane; q < G; q += 32)
+        ssq_merge(m, s, ld_cg(&a.part_nrm[q]), ld_cg(&a.part_nrm[a.gstride + q]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        R m2 = __shfl_xor_sync(0xffffffffu, m, o), s2 = __shfl_xor_sync(0xffffffffu, s, o);
+        ssq_merge(m, s, m2, s2);
       }
-      s = warp_sum(s);
       if (lane == 0) {
         R xnorm = m * sqrt(s);
         T alpha = ld_cg(&a.alpha_buf[j]);
@@ -154,16 +182,28 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
         s = fma_(conj_(v), Ps[r + c * rpc], s);
       }
       s = warp_sum(s);
-      if (lane == 0) a.part_w[b * NBMAX + c] = s;
+      if (lane == 0) a.part_w[(int64_t)c * a.gstride + b] = s;
     }
     if (!grid_barrier(a.bar, G, a.status)) return;
 
-    // ---- phase C: combine w in a fixed order, apply H_j^H to columns > j
-    for (int c = j + 1 + wid; c < jb; c += nw) {
-      T s = zero_<T>();
-      for (int q = lane; q < G; q += 32) s += ld_cg(&a.part_w[q * NBMAX + c]);
-      s = warp_sum(s);
-      if (lane == 0) wsh[c] = s;
+    // ---- phase C: combine w in a fixed order (coalesced partial rows, all
+    // loads of a warp issued before its reductions), apply H_j^H to columns > j
+    {
+      constexpr int CPW = (NBMAX + 7) / 8;  // columns per warp with 8 warps
+      T acc_c[CPW];
+#pragma unroll
+      for (int i = 0; i < CPW; i++) {
+        acc_c[i] = zero_<T>();
+        const int c = j + 1 + wid + i * nw;
+        if (c < jb)
+          for (int q = lane; q < G; q += 32) acc_c[i] += ld_cg(&a.part_w[(int64_t)c * a.gstride + q]);
+      }
+#pragma unroll
+      for (int i = 0; i < CPW; i++) {
+        const int c = j + 1 + wid + i * nw;
+        T s = warp_sum(acc_c[i]);
+        if (lane == 0 && c < jb) wsh[c] = s;
+      }
     }
     __syncthreads();
     const T ctau = conj_(tau);
@@ -262,6 +302,32 @@ __global__ void __launch_bounds__(256) reduce_trmm_kernel(int jb, int nt, int sp
 }
 
 constexpr int QR_OUTER_NB = 128;  // outer block of the mixed-precision path
+constexpr int LA_PANEL_CTAS = 24;  // panel CTAs while overlapping a trailing GEMM
+
+// Side stream (highest priority, so its panel CTAs are scheduled ahead of
+// the trailing GEMM's) and events of the look-ahead; created once, on first
+// use (before any graph capture).  Calls issued from the batched driver run
+// without look-ahead (lookahead_enabled() is false on that thread).
+struct LookAhead {
+  cudaStream_t side;
+  cudaEvent_t ev_ready, ev_done;
+};
+static thread_local bool tl_no_lookahead = false;
+bool lookahead_enabled() { return !tl_no_lookahead; }
+void set_lookahead(bool on) { tl_no_lookahead = !on; }
+static LookAhead* lookahead() {
+  static LookAhead la;
+  static bool ok = false;
+  static std::once_flag f;
+  std::call_once(f, [] {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    ok = cudaStreamCreateWithPriority(&la.side, cudaStreamNonBlocking, hi) == cudaSuccess &&
+         cudaEventCreateWithFlags(&la.ev_ready, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&la.ev_done, cudaEventDisableTiming) == cudaSuccess;
+  });
+  return ok ? &la : nullptr;
+}
 
 // T factor (forward, column-wise larft) of a JB-wide block reflector from the
 // Gram matrix G = V^H V (strict upper part used) and tau:
@@ -396,11 +462,12 @@ struct PanelShape {
   size_t smem;
 };
 template <class T>
-static int panel_shape(int64_t mp, int jb, PanelShape& ps) {
+static int panel_shape(int64_t mp, int jb, PanelShape& ps, int want_ctas) {
   const int max_ctas = num_sms();
   const size_t cap = panel_slab_cap<T>();
   int64_t rpc_max = (int64_t)(cap / ((size_t)jb * sizeof(T)));
   int64_t G = ceil_div(mp, 64);
+  if (G > want_ctas) G = want_ctas;
   if (G > max_ctas) G = max_ctas;
   if (G < 1) G = 1;
   int64_t rpc = ceil_div(mp, G);
@@ -468,6 +535,16 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     }
     ozs = ar.take<char>(oz_bytes);
   }
+  // the block Gram matrix runs on the look-ahead stream: its own scratch
+  size_t gram_bytes = 0;
+  char* grams = nullptr;
+  if (mixed) {
+    Arena meas(nullptr, 0);
+    gemm_prec<T>(st, MAK_PREC_NATIVE, NBO, NBO, m, one_<T>(), opnd<T>(nullptr, 1),
+                 opnd<T>(nullptr, 1), zero_<T>(), nullptr, 1, meas, nullptr);
+    gram_bytes = meas.off + 1024;
+    grams = ar.take<char>(gram_bytes);
+  }
   if (ar.base == nullptr) return 0;
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
   int* status = &info->status;
@@ -477,86 +554,128 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   // C <- (I - V op(T) V^H) C with the tensor-core GEMMs; op(T) = T^H for the
   // factorization, T for Q formation (T is JB x JB upper, ld NBO)
   auto larfb_mixed = [&](const T* V, int64_t mp, int JB, const T* Tm, int conjtrans, T* Cm,
-                         int64_t ldc, int64_t nc) -> int {
+                         int64_t ldc, int64_t nc, cudaStream_t s) -> int {
+    if (nc <= 0) return 0;
     {
       Arena oz(ozs, oz_bytes);
-      MAK_TRY(gemm_prec<T>(st, precision, JB, nc, mp, one_<T>(),
+      MAK_TRY(gemm_prec<T>(s, precision, JB, nc, mp, one_<T>(),
                            opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER), opnd<T>(Cm, ldc), zero_<T>(),
                            Wm, JB, oz, status));
     }
     {
       Arena oz(ozs, oz_bytes);
-      MAK_TRY(gemm_prec<T>(st, precision, JB, nc, JB, one_<T>(),
+      MAK_TRY(gemm_prec<T>(s, precision, JB, nc, JB, one_<T>(),
                            opnd<T>(Tm, NBO, conjtrans ? OP_C : OP_N, MASK_UPPER),
                            opnd<T>(Wm, JB), zero_<T>(), W2m, JB, oz, status));
     }
     Arena oz(ozs, oz_bytes);
-    return gemm_prec<T>(st, precision, mp, nc, JB, -one_<T>(),
+    return gemm_prec<T>(s, precision, mp, nc, JB, -one_<T>(),
                         opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), opnd<T>(W2m, JB), one_<T>(), Cm,
                         ldc, oz, status);
   };
+  // C = A[j0:, c0:c1] <- (I - V T^H V^H)... with the native SIMT kernels
+  auto larfb_native = [&](int64_t j0, int jb, const T* Tb, int64_t c0, int64_t c1,
+                          cudaStream_t s) -> int {
+    const int64_t nt = c1 - c0;
+    if (nt <= 0) return 0;
+    const int64_t mp = m - j0;
+    const T* Ap = A + j0 + j0 * lda;
+    T* C = A + j0 + c0 * lda;
+    int splits = pick_splits(jb, nt, mp, sms);
+    if (splits > max_splits) splits = max_splits;
+    int used = 1;
+    MAK_TRY(gemm<T>(s, jb, nt, mp, one_<T>(), opnd<T>(Ap, lda, OP_C, MASK_UNIT_LOWER),
+                    opnd<T>(C, lda), zero_<T>(), Wpart, jb, splits, (int64_t)jb * nt, &used));
+    note_launch();
+    reduce_trmm_kernel<T><<<(unsigned)ceil_div(nt, 32), 256, 0, s>>>(jb, (int)nt, used, Wpart,
+                                                                      (int64_t)jb * nt, Tb, 1, W2);
+    MAK_CUDA_TRY(cudaGetLastError());
+    return gemm<T>(s, mp, nt, jb, -one_<T>(), opnd<T>(Ap, lda, OP_N, MASK_UNIT_LOWER),
+                   opnd<T>(W2, jb), one_<T>(), C, lda);
+  };
+  // one 32-wide panel (cooperative launch)
+  // on the look-ahead stream the panel takes a few SMs only, leaving the
+  // rest to the trailing GEMM it overlaps with
+  auto panel = [&](int64_t j0, int jb, cudaStream_t s) -> int {
+    const int64_t mp = m - j0;
+    PanelShape ps;
+    MAK_TRY(panel_shape<T>(mp, jb, ps, s == st ? sms : LA_PANEL_CTAS));
+    PanelArgs<T> pa{A + j0 + j0 * lda, lda, (int)mp, jb, ps.rpc, tau + j0,
+                    Ts + (j0 / nb) * NBMAX * NBMAX, part_nrm, part_w, part_g, alpha_buf, bar,
+                    status, gmax};
+    void* args[] = {&pa};
+    ProfScope prof(s, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
+    note_launch();
+    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)qr_panel_kernel<T>, dim3(ps.G),
+                                             dim3(PANEL_THREADS), args, ps.smem, s));
+    return 0;
+  };
+  // factor outer block b: its panels with updates confined to the block,
+  // and (mixed) the 128-wide T factor from the block's Gram matrix
+  auto factor_block = [&](int64_t b, cudaStream_t s) -> int {
+    const int64_t J0 = b * NBO;
+    const int JB = (int)((k - J0) < NBO ? (k - J0) : NBO);
+    for (int64_t j0 = J0; j0 < J0 + JB; j0 += nb) {
+      const int jb = (int)((J0 + JB - j0) < nb ? (J0 + JB - j0) : nb);
+      MAK_TRY(panel(j0, jb, s));
+      MAK_TRY(larfb_native(j0, jb, Ts + (j0 / nb) * NBMAX * NBMAX, j0 + jb, J0 + JB, s));
+    }
+    if (!mixed) return 0;
+    const T* V = A + J0 + J0 * lda;
+    {
+      // the Gram matrix fixes the orthogonality of the block reflector, so
+      // it stays in native FP64 (2 m 128^2 flops per block, split-K)
+      Arena ga(grams, gram_bytes);
+      MAK_TRY(gemm_prec<T>(s, MAK_PREC_NATIVE, JB, JB, m - J0, one_<T>(),
+                           opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER),
+                           opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), zero_<T>(), Gm, NBO, ga,
+                           status));
+    }
+    static std::once_flag lg_once;
+    std::call_once(lg_once, [] {
+      cudaFuncSetAttribute(larft_gram_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)((size_t)QR_OUTER_NB * (QR_OUTER_NB + 1) / 2 * sizeof(T)));
+    });
+    note_launch();
+    larft_gram_kernel<T><<<1, 128, (size_t)NBO * (NBO + 1) / 2 * sizeof(T), s>>>(
+        JB, Gm, NBO, tau + J0, To + b * NBO * NBO, NBO);
+    MAK_CUDA_TRY(cudaGetLastError());
+    return 0;
+  };
+  // block b's reflector applied to the columns [c0, c1)
+  auto apply_block = [&](int64_t b, int64_t c0, int64_t c1, cudaStream_t s) -> int {
+    const int64_t J0 = b * NBO;
+    const int JB = (int)((k - J0) < NBO ? (k - J0) : NBO);
+    if (mixed)
+      return larfb_mixed(A + J0 + J0 * lda, m - J0, JB, To + b * NBO * NBO, 1,
+                         A + J0 + c0 * lda, lda, c1 - c0, s);
+    return larfb_native(J0, JB, Ts + (J0 / nb) * NBMAX * NBMAX, c0, c1, s);
+  };
 
   // ------------------------------------------------------------ factor
-  for (int64_t j0 = 0; j0 < k; j0 += nb) {
-    const int jb = (int)((k - j0) < nb ? (k - j0) : nb);
-    const int64_t J0 = (j0 / NBO) * NBO;                       // enclosing outer block
-    const int JB = (int)((k - J0) < NBO ? (k - J0) : NBO);
-    const int64_t col_end = mixed ? J0 + JB : n;              // inner updates stop at the block
-    const int64_t mp = m - j0;
-    T* Ap = A + j0 + j0 * lda;
-    T* Tb = Ts + (j0 / nb) * NBMAX * NBMAX;
-    PanelShape ps;
-    MAK_TRY(panel_shape<T>(mp, jb, ps));
-    PanelArgs<T> pa{Ap, lda, (int)mp, jb, ps.rpc, tau + j0, Tb, part_nrm, part_w,
-                    part_g, alpha_buf, bar, status};
-    void* args[] = {&pa};
-    {
-      ProfScope prof(st, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
-      note_launch();
-      MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)qr_panel_kernel<T>, dim3(ps.G),
-                                               dim3(PANEL_THREADS), args, ps.smem, st));
-    }
-    const int64_t nt = col_end - j0 - jb;
-    if (nt > 0) {
-      T* C = A + j0 + (j0 + jb) * lda;
-      int splits = pick_splits(jb, nt, mp, sms);
-      if (splits > max_splits) splits = max_splits;
-      int used = 1;
-      MAK_TRY(gemm<T>(st, jb, nt, mp, one_<T>(), opnd<T>(Ap, lda, OP_C, MASK_UNIT_LOWER),
-                      opnd<T>(C, lda), zero_<T>(), Wpart, jb, splits, (int64_t)jb * nt, &used));
-      note_launch();
-      reduce_trmm_kernel<T><<<(unsigned)ceil_div(nt, 32), 256, 0, st>>>(
-          jb, (int)nt, used, Wpart, (int64_t)jb * nt, Tb, 1, W2);
-      MAK_CUDA_TRY(cudaGetLastError());
-      MAK_TRY(gemm<T>(st, mp, nt, jb, -one_<T>(), opnd<T>(Ap, lda, OP_N, MASK_UNIT_LOWER),
-                      opnd<T>(W2, jb), one_<T>(), C, lda));
-    }
-    if (mixed && j0 + jb == J0 + JB) {
-      // outer block complete: its T factor from the Gram matrix of V, then
-      // the trailing update with the 128-wide block reflector
-      const T* V = A + J0 + J0 * lda;
-      const int64_t mpo = m - J0;
-      T* Tb_o = To + (J0 / NBO) * NBO * NBO;
-      {
-        Arena oz(ozs, oz_bytes);
-        // the Gram matrix fixes the orthogonality of the block reflector, so
-        // it stays in native FP64 (2 m 128^2 flops per block, split-K)
-        MAK_TRY(gemm_prec<T>(st, MAK_PREC_NATIVE, JB, JB, mpo, one_<T>(),
-                             opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER),
-                             opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), zero_<T>(), Gm, NBO, oz,
-                             status));
-      }
-      static std::once_flag lg_once;
-      std::call_once(lg_once, [] {
-        cudaFuncSetAttribute(larft_gram_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)((size_t)QR_OUTER_NB * (QR_OUTER_NB + 1) / 2 * sizeof(T)));
-      });
-      note_launch();
-      larft_gram_kernel<T><<<1, 128, (size_t)NBO * (NBO + 1) / 2 * sizeof(T), st>>>(
-          JB, Gm, NBO, tau + J0, Tb_o, NBO);
-      MAK_CUDA_TRY(cudaGetLastError());
-      if (J0 + JB < n)
-        MAK_TRY(larfb_mixed(V, mpo, JB, Tb_o, 1, A + J0 + (J0 + JB) * lda, lda, n - J0 - JB));
+  // Look-ahead: block b's reflector is applied first to block b+1's columns;
+  // a high-priority side stream then factors block b+1 while the main stream
+  // applies block b to the remaining columns, so the latency-bound panels
+  // hide behind the large trailing GEMMs.
+  LookAhead* la = (nblk_o > 1 && lookahead_enabled() && (double)m * n >= 4.0e6) ? lookahead()
+                                                                                  : nullptr;
+  if (nblk_o > 0) MAK_TRY(factor_block(0, st));
+  for (int64_t b = 0; b < nblk_o; b++) {
+    const int64_t J0 = b * NBO;
+    const int64_t nx = J0 + ((k - J0) < NBO ? (k - J0) : NBO);          // first column of b+1
+    const bool has_next = b + 1 < nblk_o;
+    const int64_t nx_end = has_next ? nx + ((k - nx) < NBO ? (k - nx) : NBO) : nx;
+    if (has_next && la) {
+      MAK_TRY(apply_block(b, nx, nx_end, st));
+      MAK_CUDA_TRY(cudaEventRecord(la->ev_ready, st));
+      MAK_CUDA_TRY(cudaStreamWaitEvent(la->side, la->ev_ready, 0));
+      MAK_TRY(factor_block(b + 1, la->side));
+      MAK_CUDA_TRY(cudaEventRecord(la->ev_done, la->side));
+      MAK_TRY(apply_block(b, nx_end, n, st));
+      MAK_CUDA_TRY(cudaStreamWaitEvent(st, la->ev_done, 0));
+    } else {
+      MAK_TRY(apply_block(b, nx, n, st));
+      if (has_next) MAK_TRY(factor_block(b + 1, st));
     }
   }
 
@@ -587,7 +706,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
       const int64_t qt = qcols - J0;
       if (qt <= 0) continue;
       MAK_TRY(larfb_mixed(A + J0 + J0 * lda, m - J0, JB, To + bo * NBO * NBO, 0,
-                          Q + J0 + J0 * ldq, ldq, qt));
+                          Q + J0 + J0 * ldq, ldq, qt, st));
     }
     return 0;
   }

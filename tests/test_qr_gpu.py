@@ -180,3 +180,17 @@ def test_qr_full_mixed(mak, cuda):
     Qh, Rh = to_host(Q), to_host(R)
     assert O.rel_err(Rh, O.qr_full(A)[1]) <= 1e-12
     assert O.orth_error(Qh) <= 1e-13 * np.sqrt(Qh.shape[1])
+
+
+@pytest.mark.parametrize("precision", ["native", "mixed"])
+def test_qr_lookahead_path(mak, cuda, precision):
+    """Large enough (m n >= 4e6) for the look-ahead side stream: block b+1 is
+    factored while block b updates the far columns."""
+    rng = np.random.default_rng(43)
+    A = O.gaussian(rng, 2560, 1664, np.float64)
+    Q, R = mak.qr_compact(to_dev(A, cuda), precision=precision)
+    Qh, Rh = to_host(Q), to_host(R)
+    Ro = O.qr_compact(A)[1]
+    assert O.rel_err(Rh, Ro) <= 1e-12
+    assert O.qr_residual(A, Qh, Rh) <= 5e-13
+    assert O.orth_error(Qh) <= 1e-13 * np.sqrt(Qh.shape[1])
