@@ -48,7 +48,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = ("QR/polar TFLOP/s + batched solves/s, mixed vs FP64 at "
           "‖A−QR‖/‖A‖≤1e-12")
 SEED = 20260101
-OZ_PAIRS = 45  # bf16 plane products per FP64 product in the split GEMM (9 slices)
+OZ_PAIRS = 36  # bf16 plane products per FP64 product in the split GEMM (8 slices)
 
 
 def parse():
@@ -360,7 +360,7 @@ def run_gb300(args):
         peak_src = ("MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else
                     "fallback 1.7 PFLOP/s sustained bf16")
     # native: FP64 flops of the products; mixed: the bf16 tensor-core flops the
-    # split method performs (45 plane products per FP64 product, 9 slices)
+    # split method performs (36 plane products per FP64 product, 8 slices)
     tensor_work = g_work.value * (OZ_PAIRS if kind == 1 else 1)
     achieved = tensor_work / (g_ms.value / 1e3) / 1e12 if g_ms.value > 0 else 0.0
     fp64_equiv = g_work.value / (g_ms.value / 1e3) / 1e12 if g_ms.value > 0 else 0.0

@@ -6,30 +6,35 @@
 //
 // 1. Row exponents E_i (of op(A)) and column exponents F_j (of op(B)) over
 //    the whole K range: |a_ik| < 2^E_i.
-// 2. Every element is cut, with integer operations on its IEEE bits, into
-//    S = 9 signed 6-bit digits of the fixed-point value a 2^(6S - E_i):
-//        a = 2^(E_i - 6) sum_p d_p 2^(-6(p-1)),   |d_p| <= 63.
-//    Plane p stores d_p 2^(-6(p-1)) as bf16 (exact: 6 significant bits).
+// 2. Every element is rounded to the 56-bit fixed-point grid of the frame
+//    2^(E_i + 1) (one bit of headroom) and cut, with integer operations on
+//    its IEEE bits, into S = 8 balanced 7-bit digits:
+//        a = 2^(E_i + 1) sum_p d_p 2^(-7p),   |d_p| <= 64.
+//    Plane p stores d_p 2^(-7(p-1)) as bf16 (exact: 7 significant bits).
 //    Complex data is made real: op(A) -> [re | im] (K doubled) and
 //    op(B) -> [[re, im], [-im, re]] (K and N doubled).
 // 3. The tcgen05 kernel multiplies plane pairs (p, q) with p + q <= S + 1
-//    (45 bf16 GEMMs per FP64 GEMM).  All products of one group d = p + q
-//    carry the same scale 2^(-6(d-2)), so each exact group (d = 2..7, at
-//    most 6 pairs) sums EXACTLY in its fp32 TMEM accumulator over a chunk of
-//    512 of K (6 x 512 x 63^2 < 2^24); every chunk the epilogue warps convert
-//    those sums to integers and add them to an int64 fixed-point accumulator
-//    per output (exact).  The remaining groups d >= 8 (weight <= 2^-36)
-//    share one "tail" accumulator that is never flushed.  Measured on GB300,
-//    the tensor core's fp32 accumulation keeps only ~20 bits per MMA with a
-//    truncation bias, so a group is either exact or lightly weighted: with
-//    7-bit digits and d = 5 in the tail the product error was ~1e-11.  The
-//    FP64 pipe (1 TFLOP/s on GB300) only sees a handful of operations per
-//    output element in the final epilogue.
+//    (36 bf16 GEMMs per FP64 GEMM); the dropped pairs weigh <= 2^-58 of
+//    2^(E_i + F_j + 2) each.  All products of one group d = p + q carry the
+//    same scale 2^(-7(d-2)) and every group has its own fp32 TMEM
+//    accumulator (8 groups x 64 columns = the 512 TMEM columns).  A group
+//    has at most S = 8 pairs, so over a chunk of 512 of K its partial sums
+//    are integers (in its scale) of magnitude <= 8 x 512 x 64^2 = 2^24:
+//    exactly representable, so the tensor core's fp32 accumulation is
+//    EXACT (measured on GB300: fp32 accumulation is exact whenever the
+//    result is representable, and truncating otherwise, so inexact groups
+//    lose precision with a bias).  Every chunk the epilogue warps convert
+//    the group sums to integers and add them to a 92-bit fixed-point
+//    accumulator per output (int64 high part in units of 2^-21 of the
+//    group-2 scale, 28-bit low part below it): exact.  The FP64 pipe
+//    (1 TFLOP/s on GB300) only sees a handful of operations per output
+//    element in the final epilogue, which rounds once to FP64.
 //
 // Kernel shape: 128 x 64 output tile per CTA, K-step 32 (one 64-byte
 // swizzled row per operand row), 2-stage TMA pipeline of S A-plane and
-// S B-plane tiles per stage, warp-specialised: warp 4 issues TMA, warp 5
-// issues the MMAs, warps 0-3 own TMEM lanes 0-127 for the epilogue.
+// S B-plane tiles per stage, warp-specialised: warp 8 issues TMA, warp 9
+// issues the MMAs, warps 0-7 run the epilogue (warp w owns TMEM lanes
+// 32 (w mod 4) .. +31 and output columns 32 (w div 4) .. +31).
 // Every mbarrier wait is bounded; on timeout the CTA records
 // MAK_ERR_TIMEOUT, drains its in-flight copies (bounded), frees TMEM and
 // exits.  Optional split-K writes FP64 partial tiles that a reduce kernel
@@ -46,10 +51,13 @@ namespace mak {
 
 constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 32;
 constexpr int OZ_KSTEPS_PER_CHUNK = 16; // 512 of K between exact flushes
-constexpr int OZ_BITS = 6;              // bits per digit plane
+constexpr int OZ_BITS = 7;              // bits per (balanced) digit plane
 constexpr int OZ_STAGES = 2;
-constexpr int OZ_THREADS = 192;         // 4 epilogue warps + TMA warp + MMA warp
-constexpr int OZ_TMEM_COLS = 512;       // 7 accumulators x 64 columns (power-of-two alloc)
+constexpr int OZ_EPI_WARPS = 8;         // two warps per TMEM lane quadrant
+constexpr int OZ_THREADS = 32 * (OZ_EPI_WARPS + 2);  // + TMA warp + MMA warp
+constexpr int OZ_TMA_WARP = OZ_EPI_WARPS, OZ_MMA_WARP = OZ_EPI_WARPS + 1;
+constexpr int OZ_EPI_COLS = OZ_BN * 4 / OZ_EPI_WARPS;  // output columns per epilogue thread
+constexpr int OZ_TMEM_COLS = 512;       // S group accumulators x 64 columns
 constexpr long long OZ_SPIN = 1ll << 26;
 
 struct OzArgs {
@@ -139,17 +147,6 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
       smem_u32(bar))
                : "memory");
 }
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
-}
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -163,12 +160,10 @@ __device__ __forceinline__ double scale_pow2(double x, int e) {
   return __longlong_as_double(b + ((long long)e << 52));
 }
 
-// group accumulator of pair (p, q) (1-based digits): 0..4 exact groups d=2..6; 5 tail
-constexpr int OZ_EXACT = 6;                // exact groups d = 2 .. OZ_EXACT + 1
-constexpr int OZ_NGROUPS = OZ_EXACT + 1;   // + the tail
-__host__ __device__ constexpr int oz_group(int p, int q) {
-  return (p + q <= OZ_EXACT + 1) ? (p + q - 2) : OZ_EXACT;
-}
+// frame of the digits: |x| < 2^(E + OZ_HEADROOM) for the row exponent E, so
+// that the rounded 56-bit fixed-point value stays <= 2^55 and the leading
+// balanced digit <= 64
+constexpr int OZ_HEADROOM = 1;
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -186,6 +181,9 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   constexpr int A_TILE = OZ_BM * OZ_BK * 2;  // bytes per A-plane tile (8 KB)
   constexpr int B_TILE = OZ_BN * OZ_BK * 2;  // bytes per B-plane tile (4 KB)
   constexpr int STAGE = S * (A_TILE + B_TILE);
+  static_assert(S * OZ_BN <= OZ_TMEM_COLS, "one TMEM accumulator per group");
+  static_assert(S % 2 == 0 && S * OZ_KSTEPS_PER_CHUNK * OZ_BK * 64 * 64 <= (1 << 24),
+                "exact group sums over a chunk");
   extern __shared__ __align__(1024) unsigned char oz_smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)oz_smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full_bar[OZ_STAGES], empty_bar[OZ_STAGES];
@@ -205,7 +203,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       mbar_init(&empty_bar[s], 1);
     }
     mbar_init(&acc_full, 1);
-    mbar_init(&acc_empty, 128);
+    mbar_init(&acc_empty, 32 * OZ_EPI_WARPS);
     mbar_init(&drain_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -221,7 +219,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   const uint32_t tmem = tmem_base_s;
   volatile int* abort_flag = &abort_s;
 
-  if (warp == 4) {
+  if (warp == OZ_TMA_WARP) {
     // ------------------------------------------------------------ TMA producer
     if (lane == 0) {
       int issued = 0;
@@ -247,10 +245,9 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         }
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == OZ_MMA_WARP) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      bool tail_started = false;
       for (int kt = 0; kt < nkt; kt++) {
         const int s = kt % OZ_STAGES;
         const int chunk = kt / OZ_KSTEPS_PER_CHUNK;
@@ -262,27 +259,21 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         tc_fence_after();
         const uint32_t sa = smem_u32(smem + s * STAGE);
         const uint32_t sb = sa + S * A_TILE;
-        bool first_in_group[OZ_NGROUPS];
-#pragma unroll
-        for (int g = 0; g < OZ_EXACT; g++) first_in_group[g] = chunk_first;
-        first_in_group[OZ_EXACT] = !tail_started;
+        // group d = p + q accumulates in TMEM columns (d - 2) * 64 .. +63;
+        // the first MMA of a group in a chunk overwrites its accumulator
 #pragma unroll
         for (int d = 2; d <= S + 1; d++) {
 #pragma unroll
           for (int p = 1; p < d; p++) {
             const int q = d - p;
-            if (p > S || q > S) continue;
-            const int g = oz_group(p, q);
 #pragma unroll
             for (int ks = 0; ks < 2; ks++) {
               const uint64_t ad = oz_desc(sa + (p - 1) * A_TILE + ks * 32);
               const uint64_t bd = oz_desc(sb + (q - 1) * B_TILE + ks * 32);
-              umma(tmem + g * OZ_BN, ad, bd, first_in_group[g] ? 0u : 1u);
-              first_in_group[g] = false;
+              umma(tmem + (d - 2) * OZ_BN, ad, bd, (chunk_first && p == 1 && ks == 0) ? 0u : 1u);
             }
           }
         }
-        tail_started = true;
         umma_commit(&empty_bar[s]);
         const bool chunk_last = ((kt + 1) % OZ_KSTEPS_PER_CHUNK) == 0 || kt + 1 == nkt;
         if (chunk_last) umma_commit(&acc_full);
@@ -294,74 +285,78 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       }
     }
   } else {
-    // ------------------------------------------------------------ epilogue warps 0-3
-    const int r = warp * 32 + lane;  // tile row == TMEM lane
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-    long long acc[OZ_BN];
+    // ------------------------------------------------------------ epilogue warps 0-7
+    // thread: output row r (TMEM lane), columns cb .. cb + OZ_EPI_COLS - 1
+    constexpr int HG = S / 2;                  // groups d = 2 .. HG + 1 form the high part
+    constexpr int LO_BITS = OZ_BITS * HG;      // low part: 2^-LO_BITS units of the high part
+    const int r = (warp & 3) * 32 + lane;
+    const int cb = (warp >> 2) * OZ_EPI_COLS;
+    const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)cb;
+    long long hi[OZ_EPI_COLS];  // units 2^(-OZ_BITS (HG - 1)) of the group-2 scale
+    int lo[OZ_EPI_COLS];        // units 2^(-OZ_BITS (S - 1)), in [0, 2^LO_BITS)
 #pragma unroll
-    for (int c = 0; c < OZ_BN; c++) acc[c] = 0;
+    for (int c = 0; c < OZ_EPI_COLS; c++) {
+      hi[c] = 0;
+      lo[c] = 0;
+    }
     bool ok = true;
     for (int chunk = 0; chunk < nchunks && ok; chunk++) {
       ok = mbar_wait(&acc_full, chunk & 1, abort_flag, a.status);
       if (!ok) break;
       tc_fence_after();
 #pragma unroll
-      for (int c0 = 0; c0 < OZ_BN; c0 += 8) {
-        float s[OZ_EXACT][8];
+      for (int c0 = 0; c0 < OZ_EPI_COLS; c0 += 8) {
+        float s[S][8];
 #pragma unroll
-        for (int g = 0; g < OZ_EXACT; g++) tmem_ld8(lane_addr + g * OZ_BN + c0, s[g]);
+        for (int g = 0; g < S; g++) tmem_ld8(lane_addr + g * OZ_BN + c0, s[g]);
         tmem_wait_ld();
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-          // group d holds an integer times 2^(-6(d-2)) below 2^24: convert
-          // each exactly and sum in units of 2^(-6(OZ_EXACT-1)) of the
-          // group-2 scale
-          long long t = 0;
+          // group d = g + 2 holds an integer times 2^(-7g) of magnitude
+          // <= 2^24: scale by 2^(7g) (exact) and convert exactly
+          long long th = 0, tl = 0;
 #pragma unroll
-          for (int g = 0; g < OZ_EXACT; g++)
-            t += (long long)__float2int_rn(s[g][j] * (float)(1 << (OZ_BITS * g)))
-                 << (OZ_BITS * (OZ_EXACT - 1 - g));
-          acc[c0 + j] += t;
+          for (int g = 0; g < S; g++) {
+            const long long v =
+                (long long)__float2int_rn(s[g][j] * __int_as_float((127 + OZ_BITS * g) << 23));
+            if (g < HG) th += v << (OZ_BITS * (HG - 1 - g));
+            else tl += v << (OZ_BITS * (S - 1 - g));
+          }
+          tl += lo[c0 + j];
+          hi[c0 + j] += th + (tl >> LO_BITS);  // arithmetic shift: floor
+          lo[c0 + j] = (int)(tl & ((1ll << LO_BITS) - 1));
         }
       }
       tc_fence_before();
       mbar_arrive(&acc_empty);
     }
     if (ok) {
-      // final: value = 2^(E+F-12-SH) (acc + tail 2^SH), SH = 6(OZ_EXACT-1).
-      // The FP64 pipe is 1/1900 of the tensor rate, so each output costs two
-      // conversions and two FP64 FMAs; the scale alpha 2^e is built by
-      // integer exponent arithmetic.
-      constexpr int SH = OZ_BITS * (OZ_EXACT - 1);
+      // final: value = 2^(E + F + 2 HEADROOM - 2 BITS - BITS (HG - 1)) (hi + lo 2^-LO_BITS),
+      // one FP64 rounding; the scale alpha 2^e is built by integer exponent
+      // arithmetic (the FP64 pipe is 1/1900 of the tensor rate)
+      constexpr int SH = 2 * OZ_BITS + OZ_BITS * (HG - 1) - 2 * OZ_HEADROOM;
       const int gi = m0 + r;
       const int Ei = (gi < a.M) ? a.EA[gi] : 0;
       const double mult = a.part ? 1.0 : a.alpha;
       const bool beta0 = a.part != nullptr || a.beta == 0.0, beta1 = a.beta == 1.0;
 #pragma unroll
-      for (int c0 = 0; c0 < OZ_BN; c0 += 16) {
-        float tl[16];
-        tmem_ld16(lane_addr + OZ_EXACT * OZ_BN + c0, tl);
-        tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int gj = n0 + c0 + j;
-          if (gi >= a.M || gj >= a.Nl) continue;
-          // the tail carries bits below the 2^-SH unit of acc: add it in FP64
-          const double v = fma((double)tl[j], (double)(1ll << SH), (double)acc[c0 + j]);
-          const double sc = scale_pow2(mult, Ei + a.EB[gj] - 2 * OZ_BITS - SH);
-          if (a.part) {
-            a.part[(int64_t)gj * a.M + gi] = v * sc;  // split-K partial, ld = M
-            continue;
-          }
-          double* dst;
-          if (a.cpx) {
-            const int jc = gj < a.Nc ? gj : gj - a.Nc;
-            dst = a.C + 2 * ((int64_t)gi + (int64_t)jc * a.ldc) + (gj < a.Nc ? 0 : 1);
-          } else {
-            dst = a.C + (int64_t)gi + (int64_t)gj * a.ldc;
-          }
-          *dst = beta0 ? v * sc : (beta1 ? fma(v, sc, *dst) : fma(v, sc, a.beta * *dst));
+      for (int c = 0; c < OZ_EPI_COLS; c++) {
+        const int gj = n0 + cb + c;
+        if (gi >= a.M || gj >= a.Nl) continue;
+        const double v = fma((double)lo[c], 1.0 / (double)(1ll << LO_BITS), (double)hi[c]);
+        const double sc = scale_pow2(mult, Ei + a.EB[gj] - SH);
+        if (a.part) {
+          a.part[(int64_t)gj * a.M + gi] = v * sc;  // split-K partial, ld = M
+          continue;
         }
+        double* dst;
+        if (a.cpx) {
+          const int jc = gj < a.Nc ? gj : gj - a.Nc;
+          dst = a.C + 2 * ((int64_t)gi + (int64_t)jc * a.ldc) + (gj < a.Nc ? 0 : 1);
+        } else {
+          dst = a.C + (int64_t)gi + (int64_t)gj * a.ldc;
+        }
+        *dst = beta0 ? v * sc : (beta1 ? fma(v, sc, *dst) : fma(v, sc, a.beta * *dst));
       }
     }
   }
@@ -512,39 +507,55 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> s, int R, int K,
   }
   __syncthreads();
   constexpr int FB = OZ_BITS * S;  // fractional bits of the fixed-point value
-  constexpr uint32_t DMASK = (1u << OZ_BITS) - 1u;
+  constexpr long long DMASK = (1ll << OZ_BITS) - 1;
+  constexpr long long HALF = 1ll << (OZ_BITS - 1);
   const size_t plane_stride = (size_t)Rpad * Kpad;
   // each thread: one row, a pair of adjacent k
   for (int e = tid; e < 64 * 32; e += 256) {
     const int rr = e / 32, kp = (e % 32) * 2;
     const int r = r0 + rr;
     if (r >= Rpad) continue;
-    const int Er = (r < R) ? E[r] : 0;
-    uint32_t dig[2][S];
-    bool neg[2];
+    const int Fr = ((r < R) ? E[r] : 0) + OZ_HEADROOM;  // frame: |x| < 2^(Fr - 1)
+    int dig[2][S];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       const double x = tile[rr][kp + h];
       const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-      neg[h] = (b >> 63) != 0;
+      const bool neg = (b >> 63) != 0;
       int ex = (int)((b >> 52) & 0x7FF);
       unsigned long long m = b & 0x000FFFFFFFFFFFFFull;
       if (ex == 0) ex = 1; else m |= 0x0010000000000000ull;
-      const int sh = ex - 1075 + FB - Er;
-      unsigned long long f;
+      // f = |x| 2^(FB - Fr) rounded to nearest: f <= 2^(FB - 1)
+      const int sh = ex - 1075 + FB - Fr;
+      long long f;
       if ((b & 0x7FFFFFFFFFFFFFFFull) == 0) f = 0;
-      else if (sh >= 0) f = (sh >= 11) ? 0 : (m << sh);  // |x| < 2^E keeps f < 2^FB
-      else f = (-sh >= 64) ? 0 : (m >> (-sh));
+      else if (sh >= 0) f = (sh >= 11) ? 0 : (long long)(m << sh);
+      else if (-sh >= 55) f = 0;
+      else f = (long long)((m >> (-sh)) + ((m >> (-sh - 1)) & 1ull));
+      // balanced base-2^7 digits from the bottom: d_p in [-64, 63] for
+      // p >= 2, leading digit in [0, 64]
 #pragma unroll
-      for (int p = 0; p < S; p++)
-        dig[h][p] = (uint32_t)((f >> (FB - OZ_BITS * (p + 1))) & DMASK);
+      for (int p = S - 1; p >= 1; p--) {
+        long long d = f & DMASK;
+        f >>= OZ_BITS;
+        if (d >= HALF) {
+          d -= DMASK + 1;
+          f += 1;
+        }
+        dig[h][p] = (int)d;
+      }
+      dig[h][0] = (int)f;
+      if (neg) {
+#pragma unroll
+        for (int p = 0; p < S; p++) dig[h][p] = -dig[h][p];
+      }
     }
 #pragma unroll
     for (int p = 0; p < S; p++) {
-      const float sc = __int_as_float((127 - OZ_BITS * p) << 23);  // 2^(-6p)
+      const float sc = __int_as_float((127 - OZ_BITS * p) << 23);  // 2^(-7p)
       __nv_bfloat162 v;
-      v.x = __float2bfloat16_rn((neg[0] ? -1.0f : 1.0f) * (float)dig[0][p] * sc);
-      v.y = __float2bfloat16_rn((neg[1] ? -1.0f : 1.0f) * (float)dig[1][p] * sc);
+      v.x = __float2bfloat16_rn((float)dig[0][p] * sc);
+      v.y = __float2bfloat16_rn((float)dig[1][p] * sc);
       const int k = k0 + kp;
       if (k < Kpad)
         *reinterpret_cast<__nv_bfloat162*>(planes + p * plane_stride + (size_t)r * Kpad + k) = v;
@@ -599,9 +610,9 @@ static void oz_set_attr() {
   });
 }
 
-// slices: 9 (54-bit fixed point) for Float64 data, 5 (30-bit) for Float32 data
+// slices: 8 (56-bit fixed point) for Float64 data, 4 (28-bit) for Float32 data
 template <class T>
-constexpr int oz_slices() { return sizeof(real_t<T>) == 8 ? 9 : 5; }
+constexpr int oz_slices() { return sizeof(real_t<T>) == 8 ? 8 : 4; }
 
 template <class T>
 int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T> A, Operand<T> B,
