@@ -143,6 +143,29 @@ int mak_qr_full_c(int64_t m, int64_t n, void* A, int64_t lda, void* Q, int64_t l
                   void* R, int64_t ldr, const mak_qr_opts* opts, void* work,
                   size_t work_bytes, mak_info* info, mak_stream_t stream);
 
+/* qr_compact! in Float64 that allocates nothing at call time.  It has no
+ * counterpart in the reference (whose CUDA path lets CUSOLVER allocate its
+ * own workspace).  For callers that cannot allocate device memory or keep a
+ * workspace: a caller whose device memory all belongs to its own pool
+ * allocator, or a binding with nowhere to keep a buffer between calls.
+ * Same arguments, results and errors as mak_qr_compact_d without the
+ * workspace; its scratch is one fixed device array of
+ * MAK_QR_NOALLOC_SCRATCH_BYTES inside the library.
+ *  - A problem whose mak_qr_workspace size exceeds that array is rejected
+ *    with MAK_ERR_WORKSPACE before any work is queued.
+ *  - The first call on each device (made with that device current) looks up
+ *    the array's address; it must come before any stream capture starts on
+ *    that device.
+ *  - Nothing in the array has to start at zero.
+ *  - All calls on one device share the array: calls whose executions overlap
+ *    (unordered streams, or several host threads) race on it.  Order them on
+ *    one stream or with events.
+ *  - info must be a device pointer (not NULL). */
+#define MAK_QR_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
+int mak_qr_compact_d_noalloc(int64_t m, int64_t n, double* A, int64_t lda, double* Q,
+                             int64_t ldq, double* R, int64_t ldr, const mak_qr_opts* opts,
+                             mak_info* info, mak_stream_t stream);
+
 /* ----------------------------------------------------------------- GEMM ---
  * C = alpha op(A) op(B) + beta C, op in {0: N, 1: T, 2: C (conjugate
  * transpose)}.  The product kernel every factorization above uses, exposed

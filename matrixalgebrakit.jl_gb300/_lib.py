@@ -59,6 +59,10 @@ _QR_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, C.POINTER(mak_qr_opts), _p
 for _kind in ("compact", "full"):
     for _s in "dzsc":
         SIGNATURES[f"mak_qr_{_kind}_{_s}"] = (C.c_int, _QR_ARGS)
+# Float64 qr_compact! with a fixed in-library scratch array (no workspace)
+MAK_QR_NOALLOC_SCRATCH_BYTES = 32 << 20
+SIGNATURES["mak_qr_compact_d_noalloc"] = (C.c_int, [_i64, _i64, _p, _i64, _p, _i64, _p, _i64,
+                                                    C.POINTER(mak_qr_opts), _p, _p])
 SIGNATURES["mak_gemm_workspace"] = (C.c_int, [C.c_int, C.c_int, C.c_int, _i64, _i64, _i64, C.c_int,
                                               C.POINTER(_sz)])
 SIGNATURES["mak_gemm_d"] = (C.c_int, [C.c_int, C.c_int, _i64, _i64, _i64, C.c_double, _p, _i64, _p,
