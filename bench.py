@@ -49,6 +49,10 @@ METRIC = ("QR/polar TFLOP/s + batched solves/s, mixed vs FP64 at "
           "‖A−QR‖/‖A‖≤1e-12")
 SEED = 20260101
 OZ_PAIRS = 36  # bf16 plane products per FP64 product in the split GEMM (8 slices)
+# DRAM traffic of the split GEMM per launch, from one ncu capture of the
+# bench workload (dram__bytes_read.sum + dram__bytes_write.sum, averaged over
+# the launches of one factorization; summary in profiles/)
+OZ_TRAFFIC = None
 
 
 def parse():
@@ -57,7 +61,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--precision", choices=["native", "mixed"], default="native")
+    ap.add_argument("--precision", choices=["native", "mixed"], default="mixed")
+    ap.add_argument("--fp64-steps", type=int, default=2,
+                    help="timed steps of the plain FP64 kernels on the same input (0: skip)")
     ap.add_argument("--m", type=int, default=16384)
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--cpu-sample", type=str, default="8192x4096",
@@ -251,6 +257,69 @@ def config_of(args):
 
 
 # ------------------------------------------------------------ GB300 arm ---
+def _read_prof(lib, kind):
+    ms, work, cnt = C.c_double(), C.c_double(), C.c_uint64()
+    lib.mak_profile_read(kind, C.byref(ms), C.byref(work), C.byref(cnt))
+    return ms.value, work.value, int(cnt.value)
+
+
+def measure_qr(mak, lib, args, dev, dist, A_master, precision, steps, warmup, clocks=None):
+    """Time `steps` factorizations (after `warmup` untimed ones) of the
+    device-resident matrix; returns the timing, accuracy and per-kernel-class
+    device time of the timed region."""
+    import torch
+
+    alg = mak.GB300_HouseholderQR(positive=True, precision=precision)
+    A = torch.empty_like(A_master)
+    Q, R = mak.initialize_output("qr_compact_", A_master)
+
+    def step():
+        A.copy_(A_master)
+        mak.qr_compact_(A, (Q, R), alg)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(warmup):
+        step()
+    barrier()
+    if clocks is not None:
+        clocks.start()
+    launches0 = lib.mak_kernel_launches()
+    lib.mak_profile_start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    barrier()
+    lib.mak_profile_stop()
+    clk = clocks.stop() if clocks is not None else None
+    launches = int(lib.mak_kernel_launches() - launches0)
+    ms = e0.elapsed_time(e1) / steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    prof = {name: _read_prof(lib, kid) for name, kid in
+            (("gemm_native", 0), ("gemm_split_tensor", 1), ("qr_panel", 2))}
+    acc = {"qr_residual": None, "orth_abs_fro": None, "orth_rel": None,
+           "diag_R_nonnegative": None}
+    if not args.lean:
+        An = torch.linalg.norm(A_master)
+        acc["qr_residual"] = float(torch.linalg.norm(A_master - Q @ R) / An)
+        G = Q.mT.conj() @ Q
+        acc["orth_abs_fro"] = float(torch.linalg.norm(
+            G - torch.eye(G.shape[0], dtype=G.dtype, device=dev)))
+        acc["orth_rel"] = acc["orth_abs_fro"] / float(torch.linalg.norm(G))
+        del G
+        acc["diag_R_nonnegative"] = bool((torch.diagonal(R) >= 0).all())
+    return {"ms": ms, "launches": launches, "prof": prof, "acc": acc, "clocks": clk,
+            "alg": alg, "A": A, "Q": Q, "R": R}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -269,114 +338,60 @@ def run_gb300(args):
     mak = ge.load_package()
     lib = mak.library()
     m, n = args.m, args.n
-    alg = mak.GB300_HouseholderQR(positive=True, precision=args.precision)
+    flops = qr_flops(m, n)
 
     rng = np.random.default_rng(SEED + rank)
     A_host = torch.from_numpy(rng.standard_normal((n, m))).t()  # column-major view
     A_master = torch.empty((n, m), dtype=torch.float64, device=dev).t()
     A_master.copy_(A_host)
-    A = torch.empty_like(A_master)
-    Q, R = mak.initialize_output("qr_compact_", A_master)
 
-    def step():
-        A.copy_(A_master)
-        mak.qr_compact_(A, (Q, R), alg)
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    for _ in range(args.warmup):
-        step()
-    barrier()
     clocks = ClockSampler(str(torch.cuda.get_device_properties(dev).uuid))
-    clocks.start()
-    launches0 = lib.mak_kernel_launches()
-    lib.mak_profile_start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        step()
-    e1.record()
-    barrier()
-    lib.mak_profile_stop()
-    clk = clocks.stop()
-    launches = int(lib.mak_kernel_launches() - launches0)
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    flops = qr_flops(m, n)
+    r = measure_qr(mak, lib, args, dev, dist, A_master, args.precision, args.steps, args.warmup,
+                   clocks)
+    ms = r["ms"]
     value = ws * flops / (ms / 1e3) / 1e12
 
-    # dominant kernel: device time of every GEMM launch inside the timed region
-    kind = 1 if args.precision == "mixed" else 0
-    g_ms, g_work, g_cnt = C.c_double(), C.c_double(), C.c_uint64()
-    lib.mak_profile_read(kind, C.byref(g_ms), C.byref(g_work), C.byref(g_cnt))
-    p_ms, p_work, p_cnt = C.c_double(), C.c_double(), C.c_uint64()
-    lib.mak_profile_read(2, C.byref(p_ms), C.byref(p_work), C.byref(p_cnt))
-    breakdown = {}
-    for kname, kid in (("gemm_native", 0), ("gemm_split_tensor", 1), ("qr_panel", 2)):
-        k_ms, k_work, k_cnt = C.c_double(), C.c_double(), C.c_uint64()
-        lib.mak_profile_read(kid, C.byref(k_ms), C.byref(k_work), C.byref(k_cnt))
-        breakdown[kname] = {"launches": int(k_cnt.value),
-                            "ms_per_step": round(k_ms.value / args.steps, 3)}
-
-    # accuracy of the last result (checker: torch/cuBLAS FP64, outside timing)
-    res = orth_abs = orth_rel = diag_ok = None
-    if not args.lean:
-        An = torch.linalg.norm(A_master)
-        res = float(torch.linalg.norm(A_master - Q @ R) / An)
-        G = Q.mT.conj() @ Q
-        orth_abs = float(torch.linalg.norm(G - torch.eye(G.shape[0], dtype=G.dtype, device=dev)))
-        orth_rel = orth_abs / float(torch.linalg.norm(G))
-        del G
-        diag_ok = bool((torch.diagonal(R) >= 0).all())
-
-    # measured FP64 peak (cuBLAS DGEMM 8192^3, best of 5) for the native roofline
+    # dominant kernel class, timed live (CUDA events on its own stream) inside
+    # the timed region
+    mixed = args.precision == "mixed"
+    g_ms, g_work, g_cnt = r["prof"]["gemm_split_tensor" if mixed else "gemm_native"]
+    p_ms, p_work, p_cnt = r["prof"]["qr_panel"]
+    breakdown = {k: {"launches": v[2], "ms_per_step": round(v[0] / args.steps, 3)}
+                 for k, v in r["prof"].items()}
     peaks = {}
     pk_path = ROOT / "MEASURED_PEAKS.json"
     if pk_path.exists():
         peaks = json.loads(pk_path.read_text())
-    if kind == 0 and args.lean:
+    if not mixed and args.lean:
         peak, peak_src = None, "not measured (--lean)"
-    elif kind == 0:
-        X = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
-        best = 1e30
-        for _ in range(6):
-            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s0.record()
-            X @ X
-            s1.record()
-            torch.cuda.synchronize()
-            best = min(best, s0.elapsed_time(s1))
-        del X
-        peak = 2 * 8192 ** 3 / (best / 1e3) / 1e12
-        peak_src = "cuBLAS DGEMM 8192^3 measured in this run (FP64 has no MEASURED_PEAKS entry)"
+    elif not mixed:
+        peak, peak_src = dgemm_peak(dev), ("cuBLAS DGEMM 8192^3 measured in this run "
+                                           "(FP64 has no MEASURED_PEAKS entry)")
+    elif peaks:
+        peak, peak_src = float(peaks["bf16_tflops_sustained"]), \
+            "of measured: MEASURED_PEAKS.json bf16_tflops_sustained"
     else:
-        peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
-        peak_src = ("MEASURED_PEAKS.json bf16_tflops_sustained" if peaks else
-                    "fallback 1.7 PFLOP/s sustained bf16")
+        peak, peak_src = 1700.0, "of fallback: 1.7 PFLOP/s sustained bf16"
     # native: FP64 flops of the products; mixed: the bf16 tensor-core flops the
-    # split method performs (36 plane products per FP64 product, 8 slices)
-    tensor_work = g_work.value * (OZ_PAIRS if kind == 1 else 1)
-    achieved = tensor_work / (g_ms.value / 1e3) / 1e12 if g_ms.value > 0 else 0.0
-    fp64_equiv = g_work.value / (g_ms.value / 1e3) / 1e12 if g_ms.value > 0 else 0.0
+    # split method performs (OZ_PAIRS plane products per FP64 product)
+    tensor_work = g_work * (OZ_PAIRS if mixed else 1)
+    achieved = tensor_work / (g_ms / 1e3) / 1e12 if g_ms > 0 else 0.0
+    fp64_equiv = g_work / (g_ms / 1e3) / 1e12 if g_ms > 0 else 0.0
+    traffic = OZ_TRAFFIC if (mixed and OZ_TRAFFIC) else None
     roofline = {"bound": "tensor", "achieved": round(achieved, 4),
                 "peak": round(peak, 4) if peak else None,
                 "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
+                "traffic": traffic["bytes_per_launch"] if traffic else None,
+                "traffic_source": traffic["source"] if traffic else None,
                 "fp64_equivalent_tflops": round(fp64_equiv, 4),
-                "traffic": None,
-                "kernel": "gemm_kernel<double> (larfb / orgqr products)" if kind == 0
-                else "ozaki_gemm (split-bf16 tcgen05)",
-                "launches": int(g_cnt.value), "avg_launch_ms": round(g_ms.value / max(1, g_cnt.value), 4),
-                "share_of_step": round(g_ms.value / (ms * args.steps), 4),
+                "kernel": "gemm_kernel<double> (larfb / orgqr products)" if not mixed
+                else "oz_gemm_kernel<8> (split-bf16 tcgen05 larfb / orgqr products)",
+                "launches": g_cnt, "avg_launch_ms": round(g_ms / max(1, g_cnt), 4),
+                "share_of_step": round(g_ms / (ms * args.steps), 4),
                 "peak_source": peak_src,
-                "panel": {"launches": int(p_cnt.value), "ms_total": round(p_ms.value, 3),
-                          "achieved_gbs": round(p_work.value / (p_ms.value / 1e3) / 1e9, 2)
-                          if p_ms.value > 0 else None},
+                "panel": {"launches": p_cnt, "ms_total": round(p_ms, 3),
+                          "achieved_gbs": round(p_work / (p_ms / 1e3) / 1e9, 2)
+                          if p_ms > 0 else None},
                 "breakdown": breakdown}
 
     out = {
@@ -386,15 +401,15 @@ def run_gb300(args):
         "data": "synthetic iid N(0,1) (numpy default_rng, seed %d)" % SEED,
         "config": config_of(args),
         "factorizations_per_s": round(ws * 1e3 / ms, 4),
-        "accuracy": {"qr_residual": res, "orth_abs_fro": orth_abs,
-                     "orth_rel": orth_rel, "diag_R_nonnegative": diag_ok},
-        "gpu_launches": launches,
+        "accuracy": r["acc"],
+        "gpu_launches": r["launches"],
         "roofline": roofline,
-        "clocks": clk,
+        "clocks": r["clocks"],
     }
 
     # end-to-end through the public API with host buffers
     if not args.no_e2e and not args.lean:
+        A, Q, R, alg = r["A"], r["Q"], r["R"], r["alg"]
         A_pin = torch.empty((n, m), dtype=torch.float64).pin_memory().t()
         A_pin.copy_(A_host)
         Q_pin = torch.empty((Q.shape[1], Q.shape[0]), dtype=torch.float64).pin_memory().t()
@@ -407,14 +422,18 @@ def run_gb300(args):
             R_pin.copy_(R, non_blocking=True)
 
         e2e_step()
-        barrier()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
         k2 = max(1, min(args.steps, 3))
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record()
         for _ in range(k2):
             e2e_step()
         s1.record()
-        barrier()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
         ems = s0.elapsed_time(s1) / k2
         if dist is not None:
             t = torch.tensor([ems], device=dev)
@@ -425,10 +444,27 @@ def run_gb300(args):
                       "h2d_bytes_per_step": int(A.numel() * 8),
                       "d2h_bytes_per_step": int((Q.numel() + R.numel()) * 8)}
         del A_pin, Q_pin, R_pin
+    del r
 
-    # left_polar! (Newton) on the single large polar problem
+    # the plain FP64 kernels on the same input: the comparison the metric asks for
+    if mixed and not args.lean and args.fp64_steps > 0:
+        r64 = measure_qr(mak, lib, args, dev, dist, A_master, "native", args.fp64_steps, 1)
+        v64 = ws * flops / (r64["ms"] / 1e3) / 1e12
+        out["fp64"] = {"value": round(v64, 5), "unit": "TFLOP/s",
+                       "ms_per_step": round(r64["ms"], 3), "steps": args.fp64_steps,
+                       "warmup": 1, "accuracy": r64["acc"],
+                       "gemm_native_ms_per_step":
+                           round(r64["prof"]["gemm_native"][0] / args.fp64_steps, 3)}
+        out["mixed_over_fp64"] = round(value / v64, 3)
+        del r64
+
+    # left_polar! (Newton) on the single large polar problem, both precisions
     if not args.no_polar and not args.lean:
-        out["polar"] = polar_measure(mak, args, dev)
+        out["polar"] = polar_measure(mak, args, dev, args.precision)
+        if mixed and args.fp64_steps > 0:
+            p64 = polar_measure(mak, args, dev, "native")
+            out["polar_fp64"] = p64
+            out["polar"]["mixed_over_fp64"] = round(p64["ms"] / out["polar"]["ms"], 3)
     if not args.no_batched and not args.lean:
         out["batched"] = batched_measure(mak, args, dev)
 
@@ -446,6 +482,23 @@ def run_gb300(args):
     if rank == 0:
         print(json.dumps(out), flush=True)
     return 0
+
+
+def dgemm_peak(dev):
+    """Measured FP64 peak: cuBLAS DGEMM 8192^3, best of 6 (CUDA events)."""
+    import torch
+
+    X = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+    best = 1e30
+    for _ in range(6):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record()
+        X @ X
+        s1.record()
+        torch.cuda.synchronize()
+        best = min(best, s0.elapsed_time(s1))
+    del X
+    return 2 * 8192 ** 3 / (best / 1e3) / 1e12
 
 
 def batched_measure(mak, args, dev):
@@ -535,7 +588,7 @@ def batched_measure(mak, args, dev):
     return res
 
 
-def polar_measure(mak, args, dev):
+def polar_measure(mak, args, dev, precision):
     import numpy as np
     import torch
 
@@ -553,7 +606,7 @@ def polar_measure(mak, args, dev):
     A0 = torch.from_numpy(np.asfortranarray(A_np)).to(dev)
     A = torch.empty_like(A0)
     W, P = mak.polar.initialize_output(A0)
-    alg = mak.GB300_PolarNewton(precision=args.precision)
+    alg = mak.GB300_PolarNewton(precision=precision)
     info = {}
     A.copy_(A0)
     mak.left_polar_(A, (W, P), alg, _info=info)  # warm-up
@@ -570,7 +623,7 @@ def polar_measure(mak, args, dev):
     G = W.mT @ W
     orth = float(torch.linalg.norm(G - torch.eye(n, dtype=G.dtype, device=dev)))
     return {"workload": f"left_polar! PolarNewton, {n}x{n} Float64, U diag(logspace(0,-6)) V^T",
-            "precision": args.precision, "ms": round(ms, 2), "iterations": k,
+            "precision": precision, "ms": round(ms, 2), "iterations": k,
             "tflops": round(polar_flops(n, n, k) / (ms / 1e3) / 1e12, 4),
             "flop_count": "k*8n^3/3 + 2n^3 (reference PolarNewton count with its own k)",
             "back_err": back, "orth_abs_fro": orth, "orth_rel": orth / math.sqrt(n),
