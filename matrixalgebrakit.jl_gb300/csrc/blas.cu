@@ -20,19 +20,23 @@ __global__ void splitk_fold_kernel(int64_t M, int64_t N, int splits, const T* pa
   C[i + j * ldc] = out;
 }
 
+// native product: split K across CTAs when the output alone cannot fill the GPU
 template <class T>
-int gemm_prec(cudaStream_t st, int precision, int64_t M, int64_t N, int64_t K, T alpha,
-              Operand<T> A, Operand<T> B, T beta, T* C, int64_t ldc, Arena& ar, int* status) {
-  if constexpr (sizeof(real_t<T>) == 8) {
-    if (precision == MAK_PREC_MIXED && im_(alpha) == 0 && im_(beta) == 0 && K >= 16)
-      return oz_gemm<T>(st, M, N, K, alpha, A, B, beta, C, ldc, ar, status);
-  }
-  // native: split K across CTAs when the output alone cannot fill the GPU
+static int gemm_native(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T> A,
+                       Operand<T> B, T beta, T* C, int64_t ldc, Arena& ar) {
   const int splits = (M > 0 && N > 0 && K > 0) ? pick_splits(M, N, K, num_sms()) : 1;
-  if (splits <= 1) {
-    if (ar.base == nullptr) return 0;
-    return gemm<T>(st, M, N, K, alpha, A, B, beta, C, ldc);
+  if (ar.base == nullptr) {
+    // measuring: a bound valid for every smaller output too (pick_splits
+    // keeps splits * tiles <= 4 * SMs), since the split count grows as the
+    // output shrinks while call sites measure at their largest shape
+    if (K > 256) {
+      const size_t bound = (size_t)4 * num_sms() * 64 * 64;
+      const size_t cap = (size_t)64 * (size_t)(M > 0 ? M : 1) * (size_t)(N > 0 ? N : 1);
+      ar.take<T>(bound < cap ? bound : cap);
+    }
+    return 0;
   }
+  if (splits <= 1) return gemm<T>(st, M, N, K, alpha, A, B, beta, C, ldc);
   T* part = ar.take<T>((size_t)splits * M * N);
   if (ar.base == nullptr) return 0;
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
@@ -44,9 +48,38 @@ int gemm_prec(cudaStream_t st, int precision, int64_t M, int64_t N, int64_t K, T
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
 
+// Inside the factorizations MAK_PREC_MIXED takes the split product only
+// when the product is large enough to repay its fixed cost (exponent pass,
+// plane split, TMEM set-up: a few tens of microseconds); smaller products
+// stay native.  PREC_SPLIT_ALWAYS (the C-ABI GEMM) takes it at every size.
+// A measuring pass (ar.base == nullptr) reserves the larger of both paths'
+// workspace, because call sites measure at their largest shape.
+template <class T>
+int gemm_prec(cudaStream_t st, int precision, int64_t M, int64_t N, int64_t K, T alpha,
+              Operand<T> A, Operand<T> B, T beta, T* C, int64_t ldc, Arena& ar, int* status,
+              int max_ctas) {
+  if constexpr (sizeof(real_t<T>) == 8) {
+    const bool can_split = (precision == MAK_PREC_MIXED || precision == PREC_SPLIT_ALWAYS) &&
+                           im_(alpha) == 0 && im_(beta) == 0 && K >= 16;
+    if (can_split) {
+      if (ar.base == nullptr) {
+        Arena a1 = ar, a2 = ar;
+        oz_gemm<T>(st, M, N, K, alpha, A, B, beta, C, ldc, a1, status);
+        gemm_native<T>(st, M, N, K, alpha, A, B, beta, C, ldc, a2);
+        ar.off = a1.off > a2.off ? a1.off : a2.off;
+        return 0;
+      }
+      const double work = (traits<T>::cpx ? 4.0 : 1.0) * (double)M * (double)N * (double)K;
+      if (precision == PREC_SPLIT_ALWAYS || work >= SPLIT_MIN_MNK)
+        return oz_gemm<T>(st, M, N, K, alpha, A, B, beta, C, ldc, ar, status, max_ctas);
+    }
+  }
+  return gemm_native<T>(st, M, N, K, alpha, A, B, beta, C, ldc, ar);
+}
+
 #define MAK_INST_GP(T)                                                                        \
   template int gemm_prec<T>(cudaStream_t, int, int64_t, int64_t, int64_t, T, Operand<T>,      \
-                            Operand<T>, T, T*, int64_t, Arena&, int*);
+                            Operand<T>, T, T*, int64_t, Arena&, int*, int);
 MAK_INST_GP(double)
 MAK_INST_GP(float)
 MAK_INST_GP(zcomplex)
@@ -73,6 +106,7 @@ static int gemm_entry(int opA, int opB, int64_t m, int64_t n, int64_t k, T alpha
   if (precision != MAK_PREC_NATIVE && precision != MAK_PREC_MIXED) return -14;
   if (info == nullptr) return -17;
   cudaStream_t st = (cudaStream_t)stream;
+  if (precision == MAK_PREC_MIXED) precision = PREC_SPLIT_ALWAYS;  // the caller chose
   Operand<T> a = opnd<T>(A, lda, opA), b = opnd<T>(B, ldb, opB);
   {
     Arena meas(nullptr, 0);

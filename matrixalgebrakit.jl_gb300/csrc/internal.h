@@ -44,15 +44,25 @@ namespace mak {
 // Split-precision (Ozaki scheme, bf16 tcgen05) GEMM for Float64 / ComplexF64:
 // C = alpha op(A) op(B) + beta C with real alpha, beta.  Workspace from `ar`
 // (measured when ar.base == nullptr).
+// max_ctas > 0 caps the persistent grid (so that a kernel on another stream
+// keeps SMs of its own); 0 = one CTA per SM.
 template <class T>
 int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T> A, Operand<T> B,
-            T beta, T* C, int64_t ldc, Arena& ar, int* status);
+            T beta, T* C, int64_t ldc, Arena& ar, int* status, int max_ctas = 0);
+
+// Internal precision code: the split product at every size (used by the
+// C-ABI GEMM, whose caller chose the arithmetic explicitly).
+constexpr int PREC_SPLIT_ALWAYS = 3;
+// Inside the factorizations, MAK_PREC_MIXED splits products with at least
+// this many multiply-adds (complex counted 4x); smaller ones stay native.
+constexpr double SPLIT_MIN_MNK = 67108864.0;  // 2^26
 
 // Dispatch: the tensor-core split GEMM when `precision` is MAK_PREC_MIXED and
 // the element type is a Float64 type with real alpha/beta, else the native
 // SIMT GEMM.  `ar` supplies the split planes (sized by a measuring pass).
 template <class T>
 int gemm_prec(cudaStream_t st, int precision, int64_t M, int64_t N, int64_t K, T alpha,
-              Operand<T> A, Operand<T> B, T beta, T* C, int64_t ldc, Arena& ar, int* status);
+              Operand<T> A, Operand<T> B, T beta, T* C, int64_t ldc, Arena& ar, int* status,
+              int max_ctas = 0);
 
 }  // namespace mak

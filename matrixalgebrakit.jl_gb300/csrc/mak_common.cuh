@@ -127,6 +127,11 @@ __device__ __forceinline__ float shfl_xor_(float v, int m) { return __shfl_xor_s
 template <class R> __device__ __forceinline__ cplx<R> shfl_xor_(cplx<R> v, int m) {
   return {shfl_xor_(v.re, m), shfl_xor_(v.im, m)};
 }
+__device__ __forceinline__ double shfl_idx_(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ float shfl_idx_(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+template <class R> __device__ __forceinline__ cplx<R> shfl_idx_(cplx<R> v, int src) {
+  return {shfl_idx_(v.re, src), shfl_idx_(v.im, src)};
+}
 template <class T> __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int m = 16; m > 0; m >>= 1) v += shfl_xor_(v, m);

@@ -26,15 +26,19 @@
 //    lose precision with a bias).  Every chunk the epilogue warps convert
 //    the group sums to integers and add them to a 92-bit fixed-point
 //    accumulator per output (int64 high part in units of 2^-21 of the
-//    group-2 scale, 28-bit low part below it): exact.  The FP64 pipe
-//    (1 TFLOP/s on GB300) only sees a handful of operations per output
-//    element in the final epilogue, which rounds once to FP64.
+//    group-2 scale, 28-bit low part below it): exact.  The final value is
+//    rounded once to FP64 by integer operations on its bits; the FP64 pipe
+//    (about 1.6 operations per clock per SM on GB300) only sees the
+//    beta * C update.
 //
-// Kernel shape: 128 x 64 output tile per CTA, K-step 32 (one 64-byte
-// swizzled row per operand row), 2-stage TMA pipeline of S A-plane and
-// S B-plane tiles per stage, warp-specialised: warp 8 issues TMA, warp 9
+// Kernel shape: persistent grid (one CTA per SM, each looping over output
+// tiles and K splits), 128 x 64 output tile, K-step 16 (one 32-byte
+// swizzled row per operand row), 4-stage TMA pipeline of S A-plane and S
+// B-plane tiles per stage, warp-specialised: warp 8 issues TMA, warp 9
 // issues the MMAs, warps 0-7 run the epilogue (warp w owns TMEM lanes
-// 32 (w mod 4) .. +31 and output columns 32 (w div 4) .. +31).
+// 32 (w mod 4) .. +31 and output columns 32 (w div 4) .. +31).  The
+// epilogue releases the accumulators before its final FP64 assembly and C
+// update, so the next tile's MMAs overlap them.
 // Every mbarrier wait is bounded; on timeout the CTA records
 // MAK_ERR_TIMEOUT, drains its in-flight copies (bounded), frees TMEM and
 // exits.  Optional split-K writes FP64 partial tiles that a reduce kernel
@@ -49,10 +53,11 @@
 
 namespace mak {
 
-constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 32;
-constexpr int OZ_KSTEPS_PER_CHUNK = 16; // 512 of K between exact flushes
+constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 16;
+constexpr int OZ_KSTEPS_PER_CHUNK = 512 / OZ_BK;  // 512 of K between exact flushes
+constexpr int OZ_ROW_BYTES = OZ_BK * 2;           // one swizzled K row of a plane tile
 constexpr int OZ_BITS = 7;              // bits per (balanced) digit plane
-constexpr int OZ_STAGES = 2;
+constexpr int OZ_STAGES = 4;           // 4 x 48 KB: finer stages keep more loads in flight
 constexpr int OZ_EPI_WARPS = 8;         // two warps per TMEM lane quadrant
 constexpr int OZ_THREADS = 32 * (OZ_EPI_WARPS + 2);  // + TMA warp + MMA warp
 constexpr int OZ_TMA_WARP = OZ_EPI_WARPS, OZ_MMA_WARP = OZ_EPI_WARPS + 1;
@@ -61,8 +66,10 @@ constexpr int OZ_TMEM_COLS = 512;       // S group accumulators x 64 columns
 constexpr long long OZ_SPIN = 1ll << 26;
 
 struct OzArgs {
-  int M, Nl, nkt;           // logical output rows, logical output cols, K-steps (this split)
-  int kt0;                  // first K-step of this split
+  int M, Nl, nkt_total;     // logical output rows, logical output cols, K-steps in all
+  int split_steps;          // K-steps per split; split z starts at K-step z * split_steps
+  int tiles_m, tiles_n;     // output tiles (OZ_BM x OZ_BN) along M and N
+  int splits;               // K splits; work items = tiles_m * tiles_n * splits
   const int* EA;            // [Mpad]
   const int* EB;            // [Nlpad]
   double* C;                // output (FP64 view; complex: interleaved re/im)
@@ -70,24 +77,46 @@ struct OzArgs {
   int cpx;                  // complex output mapping
   int Nc;                   // complex: number of complex columns (Nl = 2 Nc)
   double alpha, beta;       // real scalars
-  double* part;             // split-K partials (nullptr: write C directly)
-  int64_t part_stride;      // per split
+  double* part;             // split-K partials (nullptr: write C directly), split z at
+  int64_t part_stride;      //   part + z * part_stride
   int* status;
 };
+
+// One work item of the persistent loop: an output tile and a K range.
+// Items are numbered tile-major (M fastest, so consecutive CTAs share the
+// B-plane tile in L2), then split.
+struct OzWork {
+  int m0, n0, kt0, nkt;
+  double* part;
+};
+__device__ __forceinline__ OzWork oz_work(const OzArgs& a, int w) {
+  const int tiles = a.tiles_m * a.tiles_n;
+  const int z = w / tiles, t = w - z * tiles;
+  OzWork o;
+  o.m0 = (t % a.tiles_m) * OZ_BM;
+  o.n0 = (t / a.tiles_m) * OZ_BN;
+  o.kt0 = z * a.split_steps;
+  o.nkt = min(a.nkt_total - o.kt0, a.split_steps);
+  o.part = a.part ? a.part + (int64_t)z * a.part_stride : nullptr;
+  return o;
+}
+
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// tcgen05 shared-memory matrix descriptor, K-major operand, 64-byte swizzle:
-// rows of 64 B, 8-row core groups 512 B apart.
+// tcgen05 shared-memory matrix descriptor, K-major operand swizzled by the
+// row width (32-byte rows: SWIZZLE_32B, 64-byte rows: SWIZZLE_64B), 8-row
+// core groups 8 rows apart.
+constexpr uint64_t oz_swizzle_code() { return OZ_ROW_BYTES == 32 ? 6 : (OZ_ROW_BYTES == 64 ? 4 : 2); }
 __device__ __forceinline__ uint64_t oz_desc(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-  d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(512 >> 4) << 32;   // stride byte offset
-  d |= (uint64_t)1 << 46;            // descriptor version (sm_100 family)
-  d |= (uint64_t)4 << 61;            // SWIZZLE_64B
+  d |= (uint64_t)1 << 16;                             // leading byte offset (unused when swizzled)
+  d |= (uint64_t)((8 * OZ_ROW_BYTES) >> 4) << 32;     // stride byte offset: 8 rows
+  d |= (uint64_t)1 << 46;                             // descriptor version (sm_100 family)
+  d |= oz_swizzle_code() << 61;
   return d;
 }
 
@@ -121,6 +150,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
   }
   return true;
 }
+// the same wait for the epilogue warps, which wait microseconds for an
+// accumulator chunk: a short sleep between polls leaves the issue slots of
+// their SM sub-partitions to the TMA and MMA warps
+__device__ __forceinline__ bool mbar_wait_backoff(uint64_t* bar, uint32_t parity,
+                                                  volatile int* abort_flag, int* status) {
+  long long spins = 0;
+  while (!mbar_try(bar, parity)) {
+    if (*abort_flag) return false;
+    if (++spins > OZ_SPIN) {
+      *abort_flag = 1;
+      atomicExch(status, MAK_ERR_TIMEOUT);
+      return false;
+    }
+    __nanosleep(100);
+  }
+  return true;
+}
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -151,35 +197,101 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// x * 2^e by integer arithmetic on the exponent field (ldexp outside the
-// normal range)
-__device__ __forceinline__ double scale_pow2(double x, int e) {
-  const long long b = __double_as_longlong(x);
-  const int ex = (int)((b >> 52) & 0x7FF);
-  if (ex == 0 || ex + e <= 0 || ex + e >= 2047) return ldexp(x, e);
-  return __longlong_as_double(b + ((long long)e << 52));
+// The double nearest to (-1)^flip (hi 2^lob + lo) 2^e2 (hi signed,
+// 0 <= lo < 2^lob, lob <= 63), rounded to nearest even, built with integer
+// operations on the 128-bit two's-complement value: GB300 issues about 1.6
+// FP64 operations per clock per SM, so the conversion, the scaling and the
+// sign of alpha stay off the FP64 pipe.  Results beyond the largest double
+// become +-inf; results below the normal range are truncated to a subnormal
+// (an absolute error below 2^-1074).
+__device__ __forceinline__ double fx_to_double(long long hi, unsigned long long lo, int lob,
+                                               int e2, bool flip) {
+  unsigned long long xl = ((unsigned long long)hi << lob) | lo;
+  unsigned long long xh = (unsigned long long)(hi >> (64 - lob));
+  bool neg = (long long)xh < 0;
+  if (neg) {
+    xl = ~xl + 1ull;
+    xh = ~xh + (xl == 0ull ? 1ull : 0ull);
+  }
+  if ((xh | xl) == 0ull) return 0.0;
+  neg = neg != flip;
+  const int lz = xh ? __clzll((long long)xh) : 64 + __clzll((long long)xl);
+  unsigned long long nh, nl;
+  if (lz >= 64) {
+    nh = xl << (lz - 64);
+    nl = 0ull;
+  } else if (lz == 0) {
+    nh = xh;
+    nl = xl;
+  } else {
+    nh = (xh << lz) | (xl >> (64 - lz));
+    nl = xl << lz;
+  }
+  unsigned long long mant = nh >> 11;  // 53 bits, leading one at bit 52
+  const unsigned long long rem = nh & 0x7FFull;
+  if (rem > 0x400ull || (rem == 0x400ull && (nl != 0ull || (mant & 1ull)))) mant += 1ull;
+  int ex = 127 - lz + e2;  // value = mant 2^(ex - 52)
+  if (mant >> 53) {
+    mant >>= 1;
+    ex += 1;
+  }
+  const unsigned long long sgn = neg ? 0x8000000000000000ull : 0ull;
+  int biased = ex + 1023;
+  unsigned long long bits;
+  if (biased >= 2047) {
+    bits = sgn | 0x7FF0000000000000ull;
+  } else if (biased <= 0) {
+    const int sh = 1 - biased;  // subnormal: exponent field 0, mantissa shifted
+    bits = sgn | (sh >= 53 ? 0ull : (mant >> sh));
+  } else {
+    bits = sgn | ((unsigned long long)biased << 52) | (mant & 0x000FFFFFFFFFFFFFull);
+  }
+  return __longlong_as_double((long long)bits);
+}
+
+// The integer k of a group sum s = k 2^(-7g) (|k| <= 2^24, so s is exact in
+// fp32 and normal or zero), read from the IEEE bits on the integer pipe.
+__device__ __forceinline__ long long group_int(float s, int g) {
+  const unsigned u = __float_as_uint(s);
+  const int e = (int)((u >> 23) & 0xFFu);
+  const int m = (int)((u & 0x7FFFFFu) | 0x800000u);
+  const int sh = e - 150 + OZ_BITS * g;  // k = m 2^sh, sh in [-23, 1] for k != 0
+  int k = sh >= 0 ? (m << sh) : (m >> (-sh));
+  k = e == 0 ? 0 : k;
+  return (long long)((u >> 31) ? -k : k);
 }
 
 // frame of the digits: |x| < 2^(E + OZ_HEADROOM) for the row exponent E, so
 // that the rounded 56-bit fixed-point value stays <= 2^55 and the leading
 // balanced digit <= 64
 constexpr int OZ_HEADROOM = 1;
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                 "=r"(r[6]), "=r"(r[7])
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(taddr));
 #pragma unroll
-  for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
+  for (int j = 0; j < 4; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// address of output (gi, gj) of the logical real product (complex: column
+// gj < Nc is the real part of complex column gj, else the imaginary part of
+// column gj - Nc)
+__device__ __forceinline__ double* oz_out_ptr(double* C, int64_t ldc, int cpx, int Nc, int gi,
+                                              int gj) {
+  if (cpx) {
+    const int jc = gj < Nc ? gj : gj - Nc;
+    return C + 2 * ((int64_t)gi + (int64_t)jc * ldc) + (gj < Nc ? 0 : 1);
+  }
+  return C + (int64_t)gi + (int64_t)gj * ldc;
 }
 
 template <int S>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
 oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                OzArgs a) {
-  constexpr int A_TILE = OZ_BM * OZ_BK * 2;  // bytes per A-plane tile (8 KB)
-  constexpr int B_TILE = OZ_BN * OZ_BK * 2;  // bytes per B-plane tile (4 KB)
+  constexpr int A_TILE = OZ_BM * OZ_ROW_BYTES;  // bytes per A-plane tile
+  constexpr int B_TILE = OZ_BN * OZ_ROW_BYTES;  // bytes per B-plane tile
   constexpr int STAGE = S * (A_TILE + B_TILE);
   static_assert(S * OZ_BN <= OZ_TMEM_COLS, "one TMEM accumulator per group");
   static_assert(S % 2 == 0 && S * OZ_KSTEPS_PER_CHUNK * OZ_BK * 64 * 64 <= (1 << 24),
@@ -192,9 +304,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   __shared__ int abort_s;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * OZ_BM, n0 = blockIdx.y * OZ_BN;
-  const int nkt = a.nkt;
-  const int nchunks = (nkt + OZ_KSTEPS_PER_CHUNK - 1) / OZ_KSTEPS_PER_CHUNK;
+  const int nwork = a.tiles_m * a.tiles_n * a.splits;
 
   if (tid == 0) {
     abort_s = 0;
@@ -219,64 +329,87 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   const uint32_t tmem = tmem_base_s;
   volatile int* abort_flag = &abort_s;
 
+  // Persistent loop: this CTA takes work items blockIdx.x, blockIdx.x +
+  // gridDim.x, ...  Stage and barrier phases run on across items, so the TMA
+  // warp streams the next item's planes while the MMAs of the current one
+  // run, and the MMA warp starts the next item as soon as the epilogue has
+  // drained the accumulators (before the epilogue's final FP64 assembly and
+  // C update).
   if (warp == OZ_TMA_WARP) {
     // ------------------------------------------------------------ TMA producer
     if (lane == 0) {
-      int issued = 0;
-      for (int kt = 0; kt < nkt; kt++) {
-        const int s = kt % OZ_STAGES;
-        if (kt >= OZ_STAGES) {
-          if (!mbar_wait(&empty_bar[s], ((kt / OZ_STAGES) - 1) & 1, abort_flag, a.status)) break;
+      int it = 0;  // K-steps issued by this CTA
+      bool live = true;
+      for (int w = blockIdx.x; w < nwork && live; w += gridDim.x) {
+        const OzWork o = oz_work(a, w);
+        for (int kt = 0; kt < o.nkt; kt++, it++) {
+          const int s = it % OZ_STAGES;
+          if (it >= OZ_STAGES &&
+              !mbar_wait(&empty_bar[s], ((it / OZ_STAGES) - 1) & 1, abort_flag, a.status)) {
+            live = false;
+            break;
+          }
+          unsigned char* st = smem + s * STAGE;
+          mbar_expect_tx(&full_bar[s], STAGE);
+          const int kc = (o.kt0 + kt) * OZ_BK;
+#pragma unroll
+          for (int p = 0; p < S; p++) tma_load_3d(st + p * A_TILE, &tmA, &full_bar[s], kc, o.m0, p);
+#pragma unroll
+          for (int q = 0; q < S; q++)
+            tma_load_3d(st + S * A_TILE + q * B_TILE, &tmB, &full_bar[s], kc, o.n0, q);
         }
-        unsigned char* st = smem + s * STAGE;
-        mbar_expect_tx(&full_bar[s], STAGE);
-        const int kc = (a.kt0 + kt) * OZ_BK;
-#pragma unroll
-        for (int p = 0; p < S; p++) tma_load_3d(st + p * A_TILE, &tmA, &full_bar[s], kc, m0, p);
-#pragma unroll
-        for (int q = 0; q < S; q++)
-          tma_load_3d(st + S * A_TILE + q * B_TILE, &tmB, &full_bar[s], kc, n0, q);
-        issued = kt + 1;
       }
       // drain: every issued stage must have landed before the CTA can exit
-      for (int kt = (issued > OZ_STAGES ? issued - OZ_STAGES : 0); kt < issued; kt++) {
+      for (int k = (it > OZ_STAGES ? it - OZ_STAGES : 0); k < it; k++) {
         long long spins = 0;
-        while (!mbar_try(&full_bar[kt % OZ_STAGES], (kt / OZ_STAGES) & 1) && ++spins < OZ_SPIN) {
+        while (!mbar_try(&full_bar[k % OZ_STAGES], (k / OZ_STAGES) & 1) && ++spins < OZ_SPIN) {
         }
       }
     }
   } else if (warp == OZ_MMA_WARP) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      for (int kt = 0; kt < nkt; kt++) {
-        const int s = kt % OZ_STAGES;
-        const int chunk = kt / OZ_KSTEPS_PER_CHUNK;
-        const bool chunk_first = (kt % OZ_KSTEPS_PER_CHUNK) == 0;
-        if (chunk_first && chunk > 0) {
-          if (!mbar_wait(&acc_empty, (chunk - 1) & 1, abort_flag, a.status)) break;
-        }
-        if (!mbar_wait(&full_bar[s], (kt / OZ_STAGES) & 1, abort_flag, a.status)) break;
-        tc_fence_after();
-        const uint32_t sa = smem_u32(smem + s * STAGE);
-        const uint32_t sb = sa + S * A_TILE;
-        // group d = p + q accumulates in TMEM columns (d - 2) * 64 .. +63;
-        // the first MMA of a group in a chunk overwrites its accumulator
+      int it = 0, ch = 0;  // K-steps consumed, accumulator chunks completed
+      bool live = true;
+      for (int w = blockIdx.x; w < nwork && live; w += gridDim.x) {
+        const OzWork o = oz_work(a, w);
+        for (int kt = 0; kt < o.nkt; kt++, it++) {
+          const int s = it % OZ_STAGES;
+          const bool chunk_first = (kt % OZ_KSTEPS_PER_CHUNK) == 0;
+          if (chunk_first && ch > 0 && !mbar_wait(&acc_empty, (ch - 1) & 1, abort_flag, a.status)) {
+            live = false;
+            break;
+          }
+          if (!mbar_wait(&full_bar[s], (it / OZ_STAGES) & 1, abort_flag, a.status)) {
+            live = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sa = smem_u32(smem + s * STAGE);
+          const uint32_t sb = sa + S * A_TILE;
+          // group d = p + q accumulates in TMEM columns (d - 2) * 64 .. +63;
+          // the first MMA of a group in a chunk overwrites its accumulator
 #pragma unroll
-        for (int d = 2; d <= S + 1; d++) {
+          for (int d = 2; d <= S + 1; d++) {
 #pragma unroll
-          for (int p = 1; p < d; p++) {
-            const int q = d - p;
+            for (int p = 1; p < d; p++) {
+              const int q = d - p;
 #pragma unroll
-            for (int ks = 0; ks < 2; ks++) {
-              const uint64_t ad = oz_desc(sa + (p - 1) * A_TILE + ks * 32);
-              const uint64_t bd = oz_desc(sb + (q - 1) * B_TILE + ks * 32);
-              umma(tmem + (d - 2) * OZ_BN, ad, bd, (chunk_first && p == 1 && ks == 0) ? 0u : 1u);
+              for (int ks = 0; ks < OZ_BK / 16; ks++) {
+                const uint64_t ad = oz_desc(sa + (p - 1) * A_TILE + ks * 32);
+                const uint64_t bd = oz_desc(sb + (q - 1) * B_TILE + ks * 32);
+                umma(tmem + (d - 2) * OZ_BN, ad, bd,
+                     (chunk_first && p == 1 && ks == 0) ? 0u : 1u);
+              }
             }
           }
+          umma_commit(&empty_bar[s]);
+          const bool chunk_last = ((kt + 1) % OZ_KSTEPS_PER_CHUNK) == 0 || kt + 1 == o.nkt;
+          if (chunk_last) {
+            umma_commit(&acc_full);
+            ch++;
+          }
         }
-        umma_commit(&empty_bar[s]);
-        const bool chunk_last = ((kt + 1) % OZ_KSTEPS_PER_CHUNK) == 0 || kt + 1 == nkt;
-        if (chunk_last) umma_commit(&acc_full);
       }
       // every MMA issued must have completed before TMEM is released
       umma_commit(&drain_bar);
@@ -289,74 +422,109 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     // thread: output row r (TMEM lane), columns cb .. cb + OZ_EPI_COLS - 1
     constexpr int HG = S / 2;                  // groups d = 2 .. HG + 1 form the high part
     constexpr int LO_BITS = OZ_BITS * HG;      // low part: 2^-LO_BITS units of the high part
+    constexpr int SH = 2 * OZ_BITS + OZ_BITS * (HG - 1) - 2 * OZ_HEADROOM;
     const int r = (warp & 3) * 32 + lane;
     const int cb = (warp >> 2) * OZ_EPI_COLS;
     const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)cb;
-    long long hi[OZ_EPI_COLS];  // units 2^(-OZ_BITS (HG - 1)) of the group-2 scale
-    int lo[OZ_EPI_COLS];        // units 2^(-OZ_BITS (S - 1)), in [0, 2^LO_BITS)
-#pragma unroll
-    for (int c = 0; c < OZ_EPI_COLS; c++) {
-      hi[c] = 0;
-      lo[c] = 0;
-    }
+    int ch = 0;
     bool ok = true;
-    for (int chunk = 0; chunk < nchunks && ok; chunk++) {
-      ok = mbar_wait(&acc_full, chunk & 1, abort_flag, a.status);
-      if (!ok) break;
-      tc_fence_after();
-#pragma unroll
-      for (int c0 = 0; c0 < OZ_EPI_COLS; c0 += 8) {
-        float s[S][8];
-#pragma unroll
-        for (int g = 0; g < S; g++) tmem_ld8(lane_addr + g * OZ_BN + c0, s[g]);
-        tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          // group d = g + 2 holds an integer times 2^(-7g) of magnitude
-          // <= 2^24: scale by 2^(7g) (exact) and convert exactly
-          long long th = 0, tl = 0;
-#pragma unroll
-          for (int g = 0; g < S; g++) {
-            const long long v =
-                (long long)__float2int_rn(s[g][j] * __int_as_float((127 + OZ_BITS * g) << 23));
-            if (g < HG) th += v << (OZ_BITS * (HG - 1 - g));
-            else tl += v << (OZ_BITS * (S - 1 - g));
-          }
-          tl += lo[c0 + j];
-          hi[c0 + j] += th + (tl >> LO_BITS);  // arithmetic shift: floor
-          lo[c0 + j] = (int)(tl & ((1ll << LO_BITS) - 1));
-        }
-      }
-      tc_fence_before();
-      mbar_arrive(&acc_empty);
-    }
-    if (ok) {
-      // final: value = 2^(E + F + 2 HEADROOM - 2 BITS - BITS (HG - 1)) (hi + lo 2^-LO_BITS),
-      // one FP64 rounding; the scale alpha 2^e is built by integer exponent
-      // arithmetic (the FP64 pipe is 1/1900 of the tensor rate)
-      constexpr int SH = 2 * OZ_BITS + OZ_BITS * (HG - 1) - 2 * OZ_HEADROOM;
-      const int gi = m0 + r;
-      const int Ei = (gi < a.M) ? a.EA[gi] : 0;
-      const double mult = a.part ? 1.0 : a.alpha;
-      const bool beta0 = a.part != nullptr || a.beta == 0.0, beta1 = a.beta == 1.0;
+    for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+      const OzWork o = oz_work(a, w);
+      const int nchunks = (o.nkt + OZ_KSTEPS_PER_CHUNK - 1) / OZ_KSTEPS_PER_CHUNK;
+      double* const part = o.part;
+      const bool beta0 = part != nullptr || a.beta == 0.0, beta1 = a.beta == 1.0;
+      const int gi = o.m0 + r, n0 = o.n0;
+      double* const Cp = a.C;
+      const int64_t ldc = a.ldc;
+      const int cpx = a.cpx, Nc = a.Nc;
+      long long hi[OZ_EPI_COLS];  // units 2^(-OZ_BITS (HG - 1)) of the group-2 scale
+      int lo[OZ_EPI_COLS];        // units 2^(-OZ_BITS (S - 1)), in [0, 2^LO_BITS)
 #pragma unroll
       for (int c = 0; c < OZ_EPI_COLS; c++) {
-        const int gj = n0 + cb + c;
-        if (gi >= a.M || gj >= a.Nl) continue;
-        const double v = fma((double)lo[c], 1.0 / (double)(1ll << LO_BITS), (double)hi[c]);
-        const double sc = scale_pow2(mult, Ei + a.EB[gj] - SH);
-        if (a.part) {
-          a.part[(int64_t)gj * a.M + gi] = v * sc;  // split-K partial, ld = M
-          continue;
+        hi[c] = 0;
+        lo[c] = 0;
+      }
+      for (int chunk = 0; chunk < nchunks; chunk++, ch++) {
+        if (chunk == nchunks - 1 && !beta0 && gi < a.M) {
+          // the C tile is read once, after the last chunk: pull it into L2
+          // while the chunk's MMAs run
+#pragma unroll 4
+          for (int c = 0; c < OZ_EPI_COLS; c++) {
+            const int gj = n0 + cb + c;
+            if (gj < a.Nl) asm volatile("prefetch.global.L2 [%0];" ::"l"(oz_out_ptr(Cp, ldc, cpx, Nc, gi, gj)));
+          }
         }
-        double* dst;
-        if (a.cpx) {
-          const int jc = gj < a.Nc ? gj : gj - a.Nc;
-          dst = a.C + 2 * ((int64_t)gi + (int64_t)jc * a.ldc) + (gj < a.Nc ? 0 : 1);
+        ok = mbar_wait_backoff(&acc_full, ch & 1, abort_flag, a.status);
+        if (!ok) break;
+        tc_fence_after();
+        // 4 columns at a time: the register file is split over the four SM
+        // sub-partitions, so with 10 warps a thread has at most 168 registers
+#pragma unroll
+        for (int c0 = 0; c0 < OZ_EPI_COLS; c0 += 4) {
+          float sv[S][4];
+#pragma unroll
+          for (int g = 0; g < S; g++) tmem_ld4(lane_addr + g * OZ_BN + c0, sv[g]);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            // group d = g + 2 holds an integer times 2^(-7g) of magnitude
+            // <= 2^24: scale by 2^(7g) (exact) and convert exactly
+            long long th = 0, tl = 0;
+#pragma unroll
+            for (int g = 0; g < S; g++) {
+              const long long v = group_int(sv[g][j], g);
+              if (g < HG) th += v << (OZ_BITS * (HG - 1 - g));
+              else tl += v << (OZ_BITS * (S - 1 - g));
+            }
+            tl += lo[c0 + j];
+            hi[c0 + j] += th + (tl >> LO_BITS);  // arithmetic shift: floor
+            lo[c0 + j] = (int)(tl & ((1ll << LO_BITS) - 1));
+          }
+        }
+        // accumulators drained: the MMA warp may overwrite them
+        tc_fence_before();
+        mbar_arrive(&acc_empty);
+      }
+      if (ok && gi < a.M) {
+        // final: value = (hi 2^LO_BITS + lo) 2^(E_i + F_j - SH - LO_BITS) alpha,
+        // one rounding to FP64 by integer operations.  One loop per (alpha,
+        // beta) case, so that no FP64 work of the other cases is executed
+        // speculatively; C is read in batches of 8 columns.
+        const int e_row = a.EA[gi] - SH - LO_BITS;
+        const double alpha = part ? 1.0 : a.alpha;
+        const bool unit = alpha == 1.0 || alpha == -1.0;
+        const bool flip = alpha == -1.0;
+        const int mode = part ? 0 : (!unit ? 3 : (beta0 ? 0 : (beta1 ? 1 : 2)));
+        if (mode == 0) {
+#pragma unroll
+          for (int c = 0; c < OZ_EPI_COLS; c++) {
+            const int gj = n0 + cb + c;
+            if (gj >= a.Nl) continue;
+            const double v = fx_to_double(hi[c], (unsigned)lo[c], LO_BITS, e_row + a.EB[gj], flip);
+            if (part) part[(int64_t)gj * a.M + gi] = v;  // split-K partial, ld = M
+            else *oz_out_ptr(Cp, ldc, cpx, Nc, gi, gj) = v;
+          }
         } else {
-          dst = a.C + (int64_t)gi + (int64_t)gj * a.ldc;
+#pragma unroll
+          for (int c0 = 0; c0 < OZ_EPI_COLS; c0 += 8) {
+            double cv[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+              const int gj = n0 + cb + c0 + j;
+              cv[j] = gj < a.Nl ? *oz_out_ptr(Cp, ldc, cpx, Nc, gi, gj) : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+              const int c = c0 + j, gj = n0 + cb + c;
+              if (gj >= a.Nl) continue;
+              double v = fx_to_double(hi[c], (unsigned)lo[c], LO_BITS, e_row + a.EB[gj], flip);
+              if (mode == 1) v = cv[j] + v;
+              else if (mode == 2) v = fma(a.beta, cv[j], v);
+              else v = fma(alpha, v, beta0 ? 0.0 : a.beta * cv[j]);
+              *oz_out_ptr(Cp, ldc, cpx, Nc, gi, gj) = v;
+            }
+          }
         }
-        *dst = beta0 ? v * sc : (beta1 ? fma(v, sc, *dst) : fma(v, sc, a.beta * *dst));
       }
     }
   }
@@ -591,7 +759,10 @@ static int make_plane_map(CUtensorMap* map, void* base, int S, int rows_pad, int
   cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
   cuuint32_t es[3] = {1, 1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  OZ_ROW_BYTES == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                                     : (OZ_ROW_BYTES == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                                           : CU_TENSOR_MAP_SWIZZLE_128B),
                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : MAK_ERR_CUDA;
 }
@@ -616,7 +787,7 @@ constexpr int oz_slices() { return sizeof(real_t<T>) == 8 ? 8 : 4; }
 
 template <class T>
 int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T> A, Operand<T> B,
-            T beta, T* C, int64_t ldc, Arena& ar, int* status) {
+            T beta, T* C, int64_t ldc, Arena& ar, int* status, int max_ctas) {
   constexpr bool cpx = traits<T>::cpx;
   constexpr int S = oz_slices<T>();
   const int64_t Kl = cpx ? 2 * K : K;       // logical K
@@ -648,7 +819,20 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
   unsigned long long* bitsB = ar.take<unsigned long long>(Npad);
   __nv_bfloat16* PA = ar.take<__nv_bfloat16>((size_t)S * Mpad * Kpad);
   __nv_bfloat16* PB = ar.take<__nv_bfloat16>((size_t)S * Npad * Kpad);
-  double* part = splits > 1 ? ar.take<double>((size_t)splits * M * Nl) : nullptr;
+  // split-K partials; a measuring pass reserves a bound that holds for every
+  // smaller output as well (splitting happens only when tiles < SMs, and then
+  // splits * tiles < 2 * SMs), because call sites measure at their largest
+  // shape while the split count grows as the output shrinks
+  double* part = nullptr;
+  if (ar.base == nullptr) {
+    if (nkt_total > OZ_KSTEPS_PER_CHUNK) {
+      const size_t bound = (size_t)2 * num_sms() * OZ_BM * OZ_BN;
+      const size_t cap32 = (size_t)32 * Mpad * Npad;
+      ar.take<double>(bound < cap32 ? bound : cap32);
+    }
+  } else if (splits > 1) {
+    part = ar.take<double>((size_t)splits * M * Nl);
+  }
   if (ar.base == nullptr) return 0;
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
   if (M <= 0 || N <= 0) return 0;
@@ -673,16 +857,19 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
   const double ar_ = re_(alpha), br_ = re_(beta);
   const double work = (cpx ? 8.0 : 2.0) * (double)M * N * K;
   ProfScope prof(st, PROF_GEMM_MIXED, work);
-  for (int sp = 0; sp < splits; sp++) {
-    const int64_t kt0 = sp * chunks_per_split * OZ_KSTEPS_PER_CHUNK;
-    int64_t nkt = chunks_per_split * OZ_KSTEPS_PER_CHUNK;
-    if (kt0 + nkt > nkt_total) nkt = nkt_total - kt0;
-    OzArgs args{(int)M, (int)Nl, (int)nkt, (int)kt0, EA, EB, (double*)C, ldc, cpx ? 1 : 0,
-                (int)N, ar_, br_, part ? part + (size_t)sp * M * Nl : nullptr, 0,
+  {
+    // persistent grid: one CTA per SM (shared memory holds one CTA), each
+    // looping over work items
+    const int split_steps = (int)(chunks_per_split * OZ_KSTEPS_PER_CHUNK);
+    const int tm = (int)(Mpad / OZ_BM), tn = (int)(Npad / OZ_BN);
+    OzArgs args{(int)M, (int)Nl, (int)nkt_total, split_steps, tm, tn, splits, EA, EB,
+                (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_, part, part ? M * Nl : 0,
                 status};
+    const int64_t nwork = (int64_t)tm * tn * splits;
+    const int cap = (max_ctas > 0 && max_ctas < num_sms()) ? max_ctas : num_sms();
+    const int grid = (int)(nwork < cap ? nwork : cap);
     note_launch();
-    oz_gemm_kernel<S><<<dim3((unsigned)(Mpad / OZ_BM), (unsigned)(Npad / OZ_BN)), OZ_THREADS,
-                        oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
+    oz_gemm_kernel<S><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
     MAK_CUDA_TRY(cudaGetLastError());
   }
   if (part) {
@@ -696,7 +883,7 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
 
 #define MAK_INST_OZ(T)                                                                        \
   template int oz_gemm<T>(cudaStream_t, int64_t, int64_t, int64_t, T, Operand<T>, Operand<T>, \
-                          T, T*, int64_t, Arena&, int*);
+                          T, T*, int64_t, Arena&, int*, int);
 MAK_INST_OZ(double)
 MAK_INST_OZ(zcomplex)
 

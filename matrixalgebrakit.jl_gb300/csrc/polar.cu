@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
   __shared__ R sv[32];
   __shared__ int si[32];
   __shared__ T prow[GJ_NB];
+  __shared__ T srow[GJ_NB];
   __shared__ int pivs;
   const int G = gridDim.x, cb = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
@@ -134,15 +135,20 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
       if (tid == 0) atomicExch(a.singular, 1);
     }
     const T dinv = inv_(d);
+    // the scaled pivot row, formed once (GB300 issues about 1.6 FP64
+    // operations per clock per SM, so the elimination keeps one FMA per
+    // element); its own column holds the new pivot-column entry 1/d
+    for (int c = tid; c < b; c += blockDim.x) srow[c] = (c == j) ? dinv : prow[c] * dinv;
+    __syncthreads();
     for (int r = tid; r < nr; r += blockDim.x) {
       const int gr = r0 + r;
       if (gr == jj) {
-        for (int c = 0; c < b; c++) Ps[r + c * rpc] = (c == j) ? dinv : prow[c] * dinv;
+        for (int c = 0; c < b; c++) Ps[r + c * rpc] = srow[c];
       } else {
         const T f = Ps[r + j * rpc];
         for (int c = 0; c < b; c++) {
           if (c == j) Ps[r + c * rpc] = -(f * dinv);
-          else Ps[r + c * rpc] -= f * (prow[c] * dinv);
+          else Ps[r + c * rpc] = fma_(-f, srow[c], Ps[r + c * rpc]);
         }
       }
     }

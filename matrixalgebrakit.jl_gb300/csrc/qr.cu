@@ -12,9 +12,10 @@
 //  1. qr_panel_kernel: ONE cooperative launch factors the (m-j0) x jb panel.
 //     Each CTA keeps a contiguous slab of panel rows resident in shared
 //     memory for the whole panel; a column costs two bounded grid barriers
-//     (reflector norm, then the w = v^H A row vector).  Norms are overflow
-//     safe (scaled sum of squares) and every cross-CTA reduction is done in
-//     a fixed order, so all CTAs derive bit-identical beta/tau.  The panel's
+//     (reflector norm, then the w = v^H A row vector).  Norms are plain sums
+//     of squares with a rescaled second pass when the largest magnitude is
+//     outside a safe range, and every cross-CTA reduction is done in a fixed
+//     order, so all CTAs derive bit-identical beta/tau.  The panel's
 //     Gram matrix V^H V is reduced at the end and CTA 0 forms the T factor
 //     (forward, column-wise larft recurrence).
 //  2. larfb on the trailing columns:  W = V^H C (split-K GEMM, V read in
@@ -44,7 +45,7 @@ struct PanelArgs {
   int rpc;              // panel rows owned by one CTA
   T* tau;               // [jb]
   T* Tm;                // [NBMAX x NBMAX], ld NBMAX
-  real_t<T>* part_nrm;  // [G][2]  (scale, scaled sum of squares)
+  real_t<T>* part_nrm;  // [3][gstride]: sums of squares, largest magnitudes, rescaled sums
   T* part_w;            // [G][NBMAX]
   T* part_g;            // [G][NBMAX*NBMAX]
   T* alpha_buf;         // [NBMAX]
@@ -53,42 +54,61 @@ struct PanelArgs {
   int gstride;          // allocation stride of the per-CTA partial rows
 };
 
-// (scale, ssq) accumulation: the represented value is scale^2 * ssq
-template <class R>
-__device__ __forceinline__ void ssq_merge(R& s, R& q, R s2, R q2) {
-  if (s2 == R(0)) return;
-  if (s < s2) {
-    const R t = s / s2;
-    q = q2 + q * t * t;
-    s = s2;
-  } else {
-    const R t = s2 / s;
-    q += q2 * t * t;
+// Column norms in the panel: a plain sum of squares (one FMA per element on
+// the FP64 pipe, which GB300 runs at about 1.6 DFMA per clock per SM) next to
+// the largest magnitude, compared as IEEE bits on the integer pipe.  When the
+// largest magnitude lies outside [2^lo, 2^hi] the squares could overflow or
+// lose precision, and the norm is recomputed from values scaled by a power
+// of two (a second, rarely taken pass).
+template <class R> struct NormKey;
+template <> struct NormKey<double> {
+  using K = unsigned long long;
+  static constexpr int lo = -500, hi = 500;
+  __device__ static K key(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
   }
+  __device__ static double val(K k) { return __longlong_as_double((long long)k); }
+};
+template <> struct NormKey<float> {
+  using K = unsigned;
+  static constexpr int lo = -50, hi = 50;
+  __device__ static K key(float x) { return __float_as_uint(x) & 0x7FFFFFFFu; }
+  __device__ static float val(K k) { return __uint_as_float(k); }
+};
+template <class R> __device__ __forceinline__ typename NormKey<R>::K mag_key(R x) {
+  return NormKey<R>::key(x);
 }
-template <class R> __device__ __forceinline__ void ssq_add(R& s, R& q, R x) {
-  ssq_merge(s, q, fabs(x), x != R(0) ? R(1) : R(0));
+template <class R> __device__ __forceinline__ typename NormKey<R>::K mag_key(cplx<R> x) {
+  const auto a = NormKey<R>::key(x.re), b = NormKey<R>::key(x.im);
+  return a > b ? a : b;
 }
-template <class R> __device__ __forceinline__ void ssq_add(R& s, R& q, cplx<R> x) {
-  ssq_add(s, q, x.re);
-  ssq_add(s, q, x.im);
+template <class R> __device__ __forceinline__ R sq_add(R s, R x) { return fma_(x, x, s); }
+template <class R> __device__ __forceinline__ R sq_add(R s, cplx<R> x) {
+  return fma_(x.re, x.re, fma_(x.im, x.im, s));
 }
-// block-wide (scale, ssq) combine, result in every thread (fixed order)
-template <class R, class T>
-__device__ __forceinline__ void ssq_block(R& s, R& q, R* sh_s, T* sh_q_raw) {
-  R* sh_q = reinterpret_cast<R*>(sh_q_raw);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+template <class R> __device__ __forceinline__ void ssq_scaled_add(R& s, R x, R scale) {
+  const R y = x * scale;
+  s = fma_(y, y, s);
+}
+template <class R> __device__ __forceinline__ void ssq_scaled_add(R& s, cplx<R> x, R scale) {
+  ssq_scaled_add(s, x.re, scale);
+  ssq_scaled_add(s, x.im, scale);
+}
+template <class K> __device__ __forceinline__ K warp_max_key(K v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    R s2 = __shfl_xor_sync(0xffffffffu, s, o), q2 = __shfl_xor_sync(0xffffffffu, q, o);
-    ssq_merge(s, q, s2, q2);
+    const K w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
   }
-  __syncthreads();
-  if (lane == 0) { sh_s[wid] = s; sh_q[wid] = q; }
-  __syncthreads();
-  s = R(0);
-  q = R(0);
-  for (int w = 0; w < nw; w++) ssq_merge(s, q, sh_s[w], sh_q[w]);
+  return v;
+}
+// 0: the plain sum of squares is accurate; 1: rescale first
+template <class R> __device__ __forceinline__ int norm_needs_rescale(typename NormKey<R>::K m) {
+  using NK = NormKey<R>;
+  if (m == 0) return 0;
+  const R v = NK::val(m);
+  if (!(v < R(INFINITY))) return 0;  // Inf / NaN propagate through the plain sum
+  return (v < ldexp(R(1), NK::lo) || v > ldexp(R(1), NK::hi)) ? 1 : 0;
 }
 
 // beta / tau / 1/(alpha-beta) of one reflector, LAPACK ?larfg convention:
@@ -117,7 +137,9 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x jb, column-major, ld = rpc
   __shared__ R red_r[32];
-  __shared__ T red_t[32];
+  __shared__ typename NormKey<R>::K red_k[32];
+  __shared__ R sc_r[3];
+  __shared__ int sc_flag;
   __shared__ T wsh[NBMAX];
   __shared__ T sc[3];
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
@@ -132,38 +154,88 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
 
   for (int j = 0; j < jb; j++) {
     T* col = Ps + j * rpc;
-    // ---- phase A: one-pass scaled sum of squares (scale, ssq) of x = column
-    // j below the diagonal (LAPACK lassq-style update, overflow safe)
+    // ---- phase A: partial sum of squares and largest magnitude of x =
+    // column j below the diagonal
+    using NK = NormKey<R>;
+    using Key = typename NK::K;
     const int rs = max(0, j + 1 - r0);
-    R scl = R(0), ssq = R(0);
-    for (int r = rs + tid; r < nr; r += blockDim.x) ssq_add(scl, ssq, col[r]);
-    ssq_block(scl, ssq, red_r, red_t);
+    R ssq = R(0);
+    Key mk = 0;
+    for (int r = rs + tid; r < nr; r += blockDim.x) {
+      const T x = col[r];
+      ssq = sq_add(ssq, x);
+      const Key k = mag_key(x);
+      mk = k > mk ? k : mk;
+    }
+    ssq = warp_sum(ssq);
+    mk = warp_max_key(mk);
+    __syncthreads();
+    if (lane == 0) {
+      red_r[wid] = ssq;
+      red_k[wid] = mk;
+    }
+    __syncthreads();
     if (tid == 0) {
-      a.part_nrm[b] = scl;
-      a.part_nrm[a.gstride + b] = ssq;
+      R s = R(0);
+      Key m = 0;
+      for (int w = 0; w < nw; w++) {
+        s += red_r[w];
+        m = red_k[w] > m ? red_k[w] : m;
+      }
+      a.part_nrm[b] = s;
+      a.part_nrm[a.gstride + b] = NK::val(m);
       if (j >= r0 && j < r0 + nr) a.alpha_buf[j] = col[j - r0];
     }
     if (!grid_barrier(a.bar, G, a.status)) return;
 
-    // ---- phase B: every CTA derives the same beta/tau from the partials
+    // ---- phase B: every CTA combines the partials in the same fixed order
+    // and so derives bit-identical beta / tau
     if (wid == 0) {
-      R m = R(0), s = R(0);
-      for (int q = lane; q < G; q += 32)
-        ssq_merge(m, s, ld_cg(&a.part_nrm[q]), ld_cg(&a.part_nrm[a.gstride + q]));
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        R m2 = __shfl_xor_sync(0xffffffffu, m, o), s2 = __shfl_xor_sync(0xffffffffu, s, o);
-        ssq_merge(m, s, m2, s2);
+      R s = R(0);
+      Key m = 0;
+      for (int q = lane; q < G; q += 32) {
+        s += ld_cg(&a.part_nrm[q]);
+        const Key k = NK::key(ld_cg(&a.part_nrm[a.gstride + q]));
+        m = k > m ? k : m;
       }
+      s = warp_sum(s);
+      m = warp_max_key(m);
       if (lane == 0) {
-        R xnorm = m * sqrt(s);
-        T alpha = ld_cg(&a.alpha_buf[j]);
-        T beta, tau, scal;
-        larfg_scalars(alpha, xnorm, beta, tau, scal);
-        sc[0] = beta;
-        sc[1] = tau;
-        sc[2] = scal;
+        sc_r[0] = s;
+        sc_r[1] = NK::val(m);
+        sc_flag = norm_needs_rescale<R>(m);
       }
+    }
+    __syncthreads();
+    R xnorm = sqrt(sc_r[0]);
+    if (sc_flag) {
+      // rare: rescale by 2^-e, e the exponent of the largest magnitude
+      // (clamped so the scale itself stays finite), then sum again
+      int e = 0;
+      frexp(sc_r[1], &e);
+      e = e > 1000 ? 1000 : (e < -1000 ? -1000 : e);
+      const R scale = ldexp(R(1), -e);
+      R ss2 = R(0);
+      for (int r = rs + tid; r < nr; r += blockDim.x) ssq_scaled_add(ss2, col[r], scale);
+      ss2 = block_sum(ss2, red_r);
+      if (tid == 0) a.part_nrm[2 * a.gstride + b] = ss2;
+      if (!grid_barrier(a.bar, G, a.status)) return;
+      if (wid == 0) {
+        R s2 = R(0);
+        for (int q = lane; q < G; q += 32) s2 += ld_cg(&a.part_nrm[2 * a.gstride + q]);
+        s2 = warp_sum(s2);
+        if (lane == 0) sc_r[2] = sqrt(s2) * ldexp(R(1), e);
+      }
+      __syncthreads();
+      xnorm = sc_r[2];
+    }
+    if (tid == 0) {
+      T alpha = ld_cg(&a.alpha_buf[j]);
+      T beta, tau, scal;
+      larfg_scalars(alpha, xnorm, beta, tau, scal);
+      sc[0] = beta;
+      sc[1] = tau;
+      sc[2] = scal;
     }
     __syncthreads();
     const T beta = sc[0], tau = sc[1], scal = sc[2];
@@ -302,7 +374,7 @@ __global__ void __launch_bounds__(256) reduce_trmm_kernel(int jb, int nt, int sp
 }
 
 constexpr int QR_OUTER_NB = 128;  // outer block of the mixed-precision path
-constexpr int LA_PANEL_CTAS = 24;  // panel CTAs while overlapping a trailing GEMM
+constexpr int LA_PANEL_CTAS = 48;  // panel CTAs while overlapping a trailing GEMM
 
 // Side stream (highest priority, so its panel CTAs are scheduled ahead of
 // the trailing GEMM's) and events of the look-ahead; created once, on first
@@ -329,33 +401,48 @@ static LookAhead* lookahead() {
   return ok ? &la : nullptr;
 }
 
-// T factor (forward, column-wise larft) of a JB-wide block reflector from the
-// Gram matrix G = V^H V (strict upper part used) and tau:
-//   T[0:j, j] = -tau_j T[0:j, 0:j] G[0:j, j],  T[j, j] = tau_j.
-// One CTA; T is kept packed upper-triangular in shared memory.
+// T factor of a JB-wide block reflector (LAPACK larft, forward, column-wise
+// storage: H_1 ... H_JB = I - V T V^H) from the Gram matrix G = V^H V and
+// tau.  T is the inverse of the upper triangular U with U_ii = 1/tau_i and
+// U_il = G_il (i < l): the larft recurrence T[0:j, j] = -tau_j T[0:j, 0:j]
+// G[0:j, j], T[j, j] = tau_j, satisfies T U = I column by column.  Every
+// column of T is therefore an independent back substitution,
+//   x_k = tau_k,   x_i = -tau_i sum_{l=i+1..k} G_il x_l   (i < k),
+// written with tau_i as a factor so that tau_i = 0 (an identity reflector)
+// zeroes its row and column of T without a division.  One warp per column;
+// lane t owns rows t, t + 32, t + 64, t + 96.
 template <class T>
-__global__ void __launch_bounds__(128) larft_gram_kernel(int jb, const T* __restrict__ G, int ldg,
+__global__ void __launch_bounds__(256) larft_cols_kernel(int jb, const T* __restrict__ G, int ldg,
                                                          const T* __restrict__ tau, T* Tout,
                                                          int ldt) {
-  extern __shared__ __align__(16) unsigned char lg_raw[];
-  T* tp = reinterpret_cast<T*>(lg_raw);  // column j at offset j(j+1)/2
-  __shared__ T tv[QR_OUTER_NB];
-  const int tid = threadIdx.x;
-  for (int j = 0; j < jb; j++) {
-    const T tj = tau[j];
-    if (tid < j) tv[tid] = -(tj * G[tid + (int64_t)j * ldg]);
-    __syncthreads();
-    if (tid < j) {
-      T s = zero_<T>();
-      for (int l = tid; l < j; l++) s = fma_(tp[l * (l + 1) / 2 + tid], tv[l], s);
-      tp[j * (j + 1) / 2 + tid] = s;
-    }
-    if (tid == 0) tp[j * (j + 1) / 2 + j] = tj;
-    __syncthreads();
+  constexpr int RPL = QR_OUTER_NB / 32;
+  const int lane = threadIdx.x & 31;
+  const int k = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (k >= jb) return;
+  T acc[RPL], x[RPL];
+#pragma unroll
+  for (int r = 0; r < RPL; r++) {
+    acc[r] = zero_<T>();
+    x[r] = zero_<T>();
   }
-  for (int e = tid; e < jb * jb; e += blockDim.x) {
-    const int i = e % jb, j = e / jb;
-    Tout[i + (int64_t)j * ldt] = (i <= j) ? tp[j * (j + 1) / 2 + i] : zero_<T>();
+  for (int l = k; l >= 0; l--) {
+    const int slot = l >> 5, owner = l & 31;
+    T mine = acc[0];
+#pragma unroll
+    for (int r = 1; r < RPL; r++)
+      if (slot == r) mine = acc[r];
+    const T xl = (l == k) ? tau[k] : shfl_idx_(-(tau[l] * mine), owner);
+#pragma unroll
+    for (int r = 0; r < RPL; r++) {
+      if (slot == r && lane == owner) x[r] = xl;
+      const int i = lane + 32 * r;
+      if (i < l) acc[r] = fma_(G[i + (int64_t)l * ldg], xl, acc[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < RPL; r++) {
+    const int i = lane + 32 * r;
+    if (i < jb) Tout[i + (int64_t)k * ldt] = (i <= k) ? x[r] : zero_<T>();
   }
 }
 
@@ -512,7 +599,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   T* sgn = ar.take<T>(k > 0 ? k : 1);
   T* Wpart = ar.take<T>((size_t)max_splits * nb * (wmax > 0 ? wmax : 1));
   T* W2 = ar.take<T>((size_t)nb * (wmax > 0 ? wmax : 1));
-  real_t<T>* part_nrm = ar.take<real_t<T>>((size_t)2 * gmax);
+  real_t<T>* part_nrm = ar.take<real_t<T>>((size_t)3 * gmax);
   T* part_w = ar.take<T>((size_t)gmax * NBMAX);
   T* part_g = ar.take<T>((size_t)gmax * NBMAX * NBMAX);
   T* alpha_buf = ar.take<T>(NBMAX);
@@ -540,7 +627,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   char* grams = nullptr;
   if (mixed) {
     Arena meas(nullptr, 0);
-    gemm_prec<T>(st, MAK_PREC_NATIVE, NBO, NBO, m, one_<T>(), opnd<T>(nullptr, 1),
+    gemm_prec<T>(st, precision, NBO, NBO, m, one_<T>(), opnd<T>(nullptr, 1),
                  opnd<T>(nullptr, 1), zero_<T>(), nullptr, 1, meas, nullptr);
     gram_bytes = meas.off + 1024;
     grams = ar.take<char>(gram_bytes);
@@ -553,25 +640,26 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
 
   // C <- (I - V op(T) V^H) C with the tensor-core GEMMs; op(T) = T^H for the
   // factorization, T for Q formation (T is JB x JB upper, ld NBO)
+  // max_ctas > 0 leaves the other SMs to the look-ahead side stream
   auto larfb_mixed = [&](const T* V, int64_t mp, int JB, const T* Tm, int conjtrans, T* Cm,
-                         int64_t ldc, int64_t nc, cudaStream_t s) -> int {
+                         int64_t ldc, int64_t nc, cudaStream_t s, int max_ctas) -> int {
     if (nc <= 0) return 0;
     {
       Arena oz(ozs, oz_bytes);
       MAK_TRY(gemm_prec<T>(s, precision, JB, nc, mp, one_<T>(),
                            opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER), opnd<T>(Cm, ldc), zero_<T>(),
-                           Wm, JB, oz, status));
+                           Wm, JB, oz, status, max_ctas));
     }
     {
       Arena oz(ozs, oz_bytes);
       MAK_TRY(gemm_prec<T>(s, precision, JB, nc, JB, one_<T>(),
                            opnd<T>(Tm, NBO, conjtrans ? OP_C : OP_N, MASK_UPPER),
-                           opnd<T>(Wm, JB), zero_<T>(), W2m, JB, oz, status));
+                           opnd<T>(Wm, JB), zero_<T>(), W2m, JB, oz, status, max_ctas));
     }
     Arena oz(ozs, oz_bytes);
     return gemm_prec<T>(s, precision, mp, nc, JB, -one_<T>(),
                         opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), opnd<T>(W2m, JB), one_<T>(), Cm,
-                        ldc, oz, status);
+                        ldc, oz, status, max_ctas);
   };
   // C = A[j0:, c0:c1] <- (I - V T^H V^H)... with the native SIMT kernels
   auto larfb_native = [&](int64_t j0, int jb, const T* Tb, int64_t c0, int64_t c1,
@@ -623,32 +711,29 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     if (!mixed) return 0;
     const T* V = A + J0 + J0 * lda;
     {
-      // the Gram matrix fixes the orthogonality of the block reflector, so
-      // it stays in native FP64 (2 m 128^2 flops per block, split-K)
+      // the Gram matrix fixes the orthogonality of the block reflector; the
+      // split-precision product is FP64-accurate, and 2 m 128^2 flops per
+      // block on the FP64 pipe would sit on the look-ahead's critical path
       Arena ga(grams, gram_bytes);
-      MAK_TRY(gemm_prec<T>(s, MAK_PREC_NATIVE, JB, JB, m - J0, one_<T>(),
+      MAK_TRY(gemm_prec<T>(s, precision, JB, JB, m - J0, one_<T>(),
                            opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER),
                            opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), zero_<T>(), Gm, NBO, ga,
-                           status));
+                           status, s == st ? 0 : LA_PANEL_CTAS));
     }
-    static std::once_flag lg_once;
-    std::call_once(lg_once, [] {
-      cudaFuncSetAttribute(larft_gram_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)((size_t)QR_OUTER_NB * (QR_OUTER_NB + 1) / 2 * sizeof(T)));
-    });
     note_launch();
-    larft_gram_kernel<T><<<1, 128, (size_t)NBO * (NBO + 1) / 2 * sizeof(T), s>>>(
-        JB, Gm, NBO, tau + J0, To + b * NBO * NBO, NBO);
+    larft_cols_kernel<T><<<(unsigned)ceil_div(JB, 8), 256, 0, s>>>(JB, Gm, NBO, tau + J0,
+                                                                  To + b * NBO * NBO, NBO);
     MAK_CUDA_TRY(cudaGetLastError());
     return 0;
   };
   // block b's reflector applied to the columns [c0, c1)
-  auto apply_block = [&](int64_t b, int64_t c0, int64_t c1, cudaStream_t s) -> int {
+  auto apply_block = [&](int64_t b, int64_t c0, int64_t c1, cudaStream_t s,
+                         int max_ctas) -> int {
     const int64_t J0 = b * NBO;
     const int JB = (int)((k - J0) < NBO ? (k - J0) : NBO);
     if (mixed)
       return larfb_mixed(A + J0 + J0 * lda, m - J0, JB, To + b * NBO * NBO, 1,
-                         A + J0 + c0 * lda, lda, c1 - c0, s);
+                         A + J0 + c0 * lda, lda, c1 - c0, s, max_ctas);
     return larfb_native(J0, JB, Ts + (J0 / nb) * NBMAX * NBMAX, c0, c1, s);
   };
 
@@ -666,15 +751,16 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     const bool has_next = b + 1 < nblk_o;
     const int64_t nx_end = has_next ? nx + ((k - nx) < NBO ? (k - nx) : NBO) : nx;
     if (has_next && la) {
-      MAK_TRY(apply_block(b, nx, nx_end, st));
+      MAK_TRY(apply_block(b, nx, nx_end, st, 0));
       MAK_CUDA_TRY(cudaEventRecord(la->ev_ready, st));
       MAK_CUDA_TRY(cudaStreamWaitEvent(la->side, la->ev_ready, 0));
       MAK_TRY(factor_block(b + 1, la->side));
       MAK_CUDA_TRY(cudaEventRecord(la->ev_done, la->side));
-      MAK_TRY(apply_block(b, nx_end, n, st));
+      // the persistent tensor-core grid leaves the side stream its SMs
+      MAK_TRY(apply_block(b, nx_end, n, st, sms - LA_PANEL_CTAS));
       MAK_CUDA_TRY(cudaStreamWaitEvent(st, la->ev_done, 0));
     } else {
-      MAK_TRY(apply_block(b, nx, n, st));
+      MAK_TRY(apply_block(b, nx, n, st, 0));
       if (has_next) MAK_TRY(factor_block(b + 1, st));
     }
   }
@@ -706,7 +792,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
       const int64_t qt = qcols - J0;
       if (qt <= 0) continue;
       MAK_TRY(larfb_mixed(A + J0 + J0 * lda, m - J0, JB, To + bo * NBO * NBO, 0,
-                          Q + J0 + J0 * ldq, ldq, qt, st));
+                          Q + J0 + J0 * ldq, ldq, qt, st, 0));
     }
     return 0;
   }

@@ -140,6 +140,35 @@ def test_qr_zero_and_rank_deficient_columns(mak, cuda):
     assert np.all(np.diagonal(Rh) >= 0)
 
 
+@pytest.mark.parametrize("dt,big", [(np.float64, 1e250), (np.complex128, 1e250),
+                                    (np.float32, 1e20), (np.complex64, 1e20)],
+                         ids=["float64", "complex128", "float32", "complex64"])
+def test_qr_extreme_column_scales(mak, cuda, dt, big):
+    """Columns scaled far outside the range where a plain sum of squares is
+    safe (squares overflow or underflow): the panel's column norms take the
+    rescaled pass.  QR is column-scale equivariant, A D = Q (R D) for a
+    positive diagonal D, so the scaled factorization must reproduce the
+    unscaled one column by column; R is also checked against the oracle."""
+    rng = np.random.default_rng(17)
+    m, n = 300, 40
+    A = O.gaussian(rng, m, n, dt)
+    rdt = np.float64 if dt in (np.float64, np.complex128) else np.float32
+    d = np.array([big, 1.0 / big, 1.0, big, 1.0 / big] * (n // 5), dtype=rdt)
+    AD = (A * d[None, :]).astype(dt)
+    Q1, R1 = mak.qr_compact(to_dev(A, cuda))
+    Q2, R2 = mak.qr_compact(to_dev(AD, cuda))
+    Q1h, R1h, Q2h, R2h = to_host(Q1), to_host(R1), to_host(Q2), to_host(R2)
+    assert np.all(np.isfinite(R2h)) and np.all(np.isfinite(Q2h))
+    t = tol(dt)
+    assert O.rel_err(Q2h, Q1h) <= 50 * t
+    for j in range(n):
+        col = R1h[:, j] * d[j]
+        assert np.linalg.norm(R2h[:, j] - col) <= 50 * t * np.linalg.norm(col)
+    Ro = O.qr_compact(AD)[1]
+    for j in range(n):
+        assert np.linalg.norm(R2h[:, j] - Ro[:, j]) <= 50 * t * np.linalg.norm(Ro[:, j])
+
+
 def test_qr_dimension_errors(mak, cuda):
     A = torch.zeros((10, 4), dtype=torch.float64, device=cuda).t().contiguous().t()
     Q = torch.zeros((4, 10), dtype=torch.float64, device=cuda).t()
