@@ -77,6 +77,11 @@ def parse():
     ap.add_argument("--polar-n", type=int, default=8192)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-blocks", type=int, default=300)
+    ap.add_argument("--workload", choices=["qr", "gemm"], default="qr",
+                    help="gemm: time the split-precision product alone on --gemm-shapes")
+    ap.add_argument("--gemm-shapes", type=str, default="16384x8192x128,128x8192x16384",
+                    help="MxNxK list for --workload gemm (the trailing-update shapes of the "
+                         "16384 x 8192 QR: C -= V W2 and W = V^H C)")
     return ap.parse_args()
 
 
@@ -630,10 +635,74 @@ def polar_measure(mak, args, dev, precision):
             "steps": 1, "warmup": 1}
 
 
+def run_gemm(args):
+    """The split-precision GEMM alone through the C ABI (mak_gemm_d, mixed):
+    C = -op(A) B + C on device-resident operands, the shapes of the QR's
+    trailing update; FP64-equivalent and bf16 tensor TFLOP/s per shape."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    mak = ge.load_package()
+    lib = mak.library()
+    from mak_gb300 import _lib
+
+    out = {"metric": "split-precision GEMM TFLOP/s (FP64-equivalent)", "unit": "TFLOP/s",
+           "dtype": "f64", "data": "synthetic iid N(0,1)", "shapes": []}
+    gen = torch.Generator(device=dev).manual_seed(SEED)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    for shape in args.gemm_shapes.split(","):
+        m, n, k = (int(x) for x in shape.split("x"))
+        opA = 2 if m <= 256 else 0  # W = V^H C reads V transposed
+        A = (torch.randn((m, k) if opA == 0 else (k, m), dtype=torch.float64, device=dev,
+                         generator=gen).t().contiguous().t())
+        B = torch.randn((n, k), dtype=torch.float64, device=dev, generator=gen).t()
+        Cm = torch.randn((n, m), dtype=torch.float64, device=dev, generator=gen).t()
+        nb = C.c_size_t()
+        lib.mak_gemm_workspace(_lib.MAK_F64, opA, 0, m, n, k, _lib.MAK_PREC_MIXED, C.byref(nb))
+        work = torch.empty(nb.value, dtype=torch.uint8, device=dev)
+        info = torch.zeros(C.sizeof(_lib.mak_info), dtype=torch.uint8, device=dev)
+        lda = A.stride(1)
+
+        def call():
+            rc = lib.mak_gemm_d(opA, 0, m, n, k, -1.0, A.data_ptr(), lda, B.data_ptr(), k, 1.0,
+                                Cm.data_ptr(), m, _lib.MAK_PREC_MIXED, work.data_ptr(), nb.value,
+                                info.data_ptr(), st)
+            assert rc == 0, lib.mak_status_string(rc)
+
+        for _ in range(max(3, args.warmup)):
+            call()
+        torch.cuda.synchronize()
+        lib.mak_profile_start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        lib.mak_profile_stop()
+        ms = e0.elapsed_time(e1) / args.steps
+        k_ms, k_work, k_cnt = _read_prof(lib, 1)
+        f64 = 2.0 * m * n * k / (ms / 1e3) / 1e12
+        kern = k_work / (k_ms / 1e3) / 1e12 if k_ms > 0 else None
+        out["shapes"].append({"m": m, "n": n, "k": k, "op_a": "CNT"[opA], "ms": round(ms, 4),
+                              "fp64_equiv_tflops": round(f64, 3),
+                              "kernel_ms": round(k_ms / max(1, k_cnt), 4),
+                              "kernel_fp64_equiv_tflops": round(kern, 3) if kern else None,
+                              "kernel_tensor_tflops": round(kern * OZ_PAIRS, 1) if kern else None})
+        del A, B, Cm, work
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "gemm":
+        return run_gemm(args)
     return run_gb300(args)
 
 

@@ -249,6 +249,14 @@ __device__ __forceinline__ double fx_to_double(long long hi, unsigned long long 
   return __longlong_as_double((long long)bits);
 }
 
+// The integer k of a group sum s = k 2^(-7g) with |k| <= 2^22: s 2^(7g) + 1.5
+// 2^23 is exact in fp32 (an integer in [2^23, 2^24]), so one FFMA and one
+// integer subtraction recover k.
+__device__ __forceinline__ int group_int_small(float s, int g) {
+  return __float_as_int(fmaf(s, __int_as_float((127 + OZ_BITS * g) << 23), 12582912.0f)) -
+         0x4B400000;
+}
+
 // The integer k of a group sum s = k 2^(-7g) (|k| <= 2^24, so s is exact in
 // fp32 and normal or zero), read from the IEEE bits on the integer pipe.
 __device__ __forceinline__ long long group_int(float s, int g) {
@@ -286,7 +294,10 @@ __device__ __forceinline__ double* oz_out_ptr(double* C, int64_t ldc, int cpx, i
   return C + (int64_t)gi + (int64_t)gj * ldc;
 }
 
-template <int S>
+// CHUNK = K-steps per exact accumulator chunk: 32 (512 of K, group sums up
+// to 2^24, converted from their bits) or 8 (128 of K, group sums up to 2^22,
+// converted with one FFMA; products with K <= 128 use this variant).
+template <int S, int CHUNK>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
 oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                OzArgs a) {
@@ -294,8 +305,9 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   constexpr int B_TILE = OZ_BN * OZ_ROW_BYTES;  // bytes per B-plane tile
   constexpr int STAGE = S * (A_TILE + B_TILE);
   static_assert(S * OZ_BN <= OZ_TMEM_COLS, "one TMEM accumulator per group");
-  static_assert(S % 2 == 0 && S * OZ_KSTEPS_PER_CHUNK * OZ_BK * 64 * 64 <= (1 << 24),
+  static_assert(S % 2 == 0 && S * CHUNK * OZ_BK * 64 * 64 <= (1 << 24),
                 "exact group sums over a chunk");
+  constexpr bool kSmallChunk = S * CHUNK * OZ_BK * 64 * 64 <= (1 << 22);
   extern __shared__ __align__(1024) unsigned char oz_smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)oz_smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full_bar[OZ_STAGES], empty_bar[OZ_STAGES];
@@ -375,7 +387,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         const OzWork o = oz_work(a, w);
         for (int kt = 0; kt < o.nkt; kt++, it++) {
           const int s = it % OZ_STAGES;
-          const bool chunk_first = (kt % OZ_KSTEPS_PER_CHUNK) == 0;
+          const bool chunk_first = (kt % CHUNK) == 0;
           if (chunk_first && ch > 0 && !mbar_wait(&acc_empty, (ch - 1) & 1, abort_flag, a.status)) {
             live = false;
             break;
@@ -404,7 +416,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             }
           }
           umma_commit(&empty_bar[s]);
-          const bool chunk_last = ((kt + 1) % OZ_KSTEPS_PER_CHUNK) == 0 || kt + 1 == o.nkt;
+          const bool chunk_last = ((kt + 1) % CHUNK) == 0 || kt + 1 == o.nkt;
           if (chunk_last) {
             umma_commit(&acc_full);
             ch++;
@@ -430,7 +442,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     bool ok = true;
     for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
       const OzWork o = oz_work(a, w);
-      const int nchunks = (o.nkt + OZ_KSTEPS_PER_CHUNK - 1) / OZ_KSTEPS_PER_CHUNK;
+      const int nchunks = (o.nkt + CHUNK - 1) / CHUNK;
       double* const part = o.part;
       const bool beta0 = part != nullptr || a.beta == 0.0, beta1 = a.beta == 1.0;
       const int gi = o.m0 + r, n0 = o.n0;
@@ -467,14 +479,25 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           tmem_wait_ld();
 #pragma unroll
           for (int j = 0; j < 4; j++) {
-            // group d = g + 2 holds an integer times 2^(-7g) of magnitude
-            // <= 2^24: scale by 2^(7g) (exact) and convert exactly
+            // group d = g + 2 holds an integer times 2^(-7g): scale by 2^(7g)
+            // (exact) and convert exactly
             long long th = 0, tl = 0;
+            if constexpr (kSmallChunk && S == 8) {
+              // |k| <= 2^22: pairs k_a 2^7 + k_b stay below 2^30 in int32
+              int k[S];
 #pragma unroll
-            for (int g = 0; g < S; g++) {
-              const long long v = group_int(sv[g][j], g);
-              if (g < HG) th += v << (OZ_BITS * (HG - 1 - g));
-              else tl += v << (OZ_BITS * (S - 1 - g));
+              for (int g = 0; g < S; g++) k[g] = group_int_small(sv[g][j], g);
+              const int p01 = k[0] * (1 << OZ_BITS) + k[1], p23 = k[2] * (1 << OZ_BITS) + k[3];
+              const int p45 = k[4] * (1 << OZ_BITS) + k[5], p67 = k[6] * (1 << OZ_BITS) + k[7];
+              th = (long long)p01 * (1ll << (2 * OZ_BITS)) + p23;
+              tl = (long long)p45 * (1ll << (2 * OZ_BITS)) + p67;
+            } else {
+#pragma unroll
+              for (int g = 0; g < S; g++) {
+                const long long v = group_int(sv[g][j], g);
+                if (g < HG) th += v << (OZ_BITS * (HG - 1 - g));
+                else tl += v << (OZ_BITS * (S - 1 - g));
+              }
             }
             tl += lo[c0 + j];
             hi[c0 + j] += th + (tl >> LO_BITS);  // arithmetic shift: floor
@@ -776,7 +799,9 @@ template <int S>
 static void oz_set_attr() {
   static std::once_flag f;
   std::call_once(f, [] {
-    cudaFuncSetAttribute(oz_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(oz_gemm_kernel<S, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)oz_smem_bytes<S>());
+    cudaFuncSetAttribute(oz_gemm_kernel<S, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)oz_smem_bytes<S>());
   });
 }
@@ -869,7 +894,10 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
     const int cap = (max_ctas > 0 && max_ctas < num_sms()) ? max_ctas : num_sms();
     const int grid = (int)(nwork < cap ? nwork : cap);
     note_launch();
-    oz_gemm_kernel<S><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
+    if (nkt_total * OZ_BK <= 128)  // one short chunk: the FFMA conversion
+      oz_gemm_kernel<S, 8><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
+    else
+      oz_gemm_kernel<S, 32><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
     MAK_CUDA_TRY(cudaGetLastError());
   }
   if (part) {

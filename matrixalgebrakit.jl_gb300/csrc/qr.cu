@@ -29,6 +29,7 @@
 #include "gemm.cuh"
 #include "internal.h"
 
+#include <cstdlib>
 #include <mutex>
 
 namespace mak {
@@ -374,7 +375,21 @@ __global__ void __launch_bounds__(256) reduce_trmm_kernel(int jb, int nt, int sp
 }
 
 constexpr int QR_OUTER_NB = 128;  // outer block of the mixed-precision path
-constexpr int LA_PANEL_CTAS = 48;  // panel CTAs while overlapping a trailing GEMM
+// SMs given to the look-ahead side stream (panels and the block Gram) while
+// the main stream's persistent tensor-core grid takes the rest; 48 by
+// default, MAK_LOOKAHEAD_CTAS overrides it (read once, clamped to 8..120).
+static int lookahead_ctas() {
+  static int v = 48;
+  static std::once_flag f;
+  std::call_once(f, [] {
+    const char* e = getenv("MAK_LOOKAHEAD_CTAS");
+    if (e && *e) {
+      const int x = atoi(e);
+      v = x < 8 ? 8 : (x > 120 ? 120 : x);
+    }
+  });
+  return v;
+}
 
 // Side stream (highest priority, so its panel CTAs are scheduled ahead of
 // the trailing GEMM's) and events of the look-ahead; created once, on first
@@ -590,7 +605,12 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   const int max_splits = 64;
   // mixed precision: 128-wide outer blocks whose block reflector is applied
   // with split-precision tensor-core GEMMs (K = 128 or K = m)
-  const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8;
+  // the 128-wide blocking pays only when its products are large enough to
+  // take the split tensor-core path (gemm_prec's threshold); smaller
+  // problems run the native blocking even when mixed precision is asked for
+  const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8 &&
+                     (traits<T>::cpx ? 4.0 : 1.0) * (double)m * (double)n * QR_OUTER_NB >=
+                         SPLIT_MIN_MNK;
   const int NBO = mixed ? QR_OUTER_NB : nb;
   const int64_t nblk_o = ceil_div(k, NBO);
 
@@ -687,7 +707,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   auto panel = [&](int64_t j0, int jb, cudaStream_t s) -> int {
     const int64_t mp = m - j0;
     PanelShape ps;
-    MAK_TRY(panel_shape<T>(mp, jb, ps, s == st ? sms : LA_PANEL_CTAS));
+    MAK_TRY(panel_shape<T>(mp, jb, ps, s == st ? sms : lookahead_ctas()));
     PanelArgs<T> pa{A + j0 + j0 * lda, lda, (int)mp, jb, ps.rpc, tau + j0,
                     Ts + (j0 / nb) * NBMAX * NBMAX, part_nrm, part_w, part_g, alpha_buf, bar,
                     status, gmax};
@@ -718,7 +738,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
       MAK_TRY(gemm_prec<T>(s, precision, JB, JB, m - J0, one_<T>(),
                            opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER),
                            opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), zero_<T>(), Gm, NBO, ga,
-                           status, s == st ? 0 : LA_PANEL_CTAS));
+                           status, s == st ? 0 : lookahead_ctas()));
     }
     note_launch();
     larft_cols_kernel<T><<<(unsigned)ceil_div(JB, 8), 256, 0, s>>>(JB, Gm, NBO, tau + J0,
@@ -757,7 +777,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
       MAK_TRY(factor_block(b + 1, la->side));
       MAK_CUDA_TRY(cudaEventRecord(la->ev_done, la->side));
       // the persistent tensor-core grid leaves the side stream its SMs
-      MAK_TRY(apply_block(b, nx_end, n, st, sms - LA_PANEL_CTAS));
+      MAK_TRY(apply_block(b, nx_end, n, st, sms - lookahead_ctas()));
       MAK_CUDA_TRY(cudaStreamWaitEvent(st, la->ev_done, 0));
     } else {
       MAK_TRY(apply_block(b, nx, n, st, 0));

@@ -113,7 +113,7 @@ def test_left_polar_errors_and_warning(mak, cuda):
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.complex128], ids=lambda d: np.dtype(d).name)
-@pytest.mark.parametrize("shape", [(300, 300), (700, 260), (512, 512)])
+@pytest.mark.parametrize("shape", [(300, 300), (700, 260), (512, 512), (768, 768)])
 def test_left_polar_mixed(mak, cuda, dt, shape):
     """precision="mixed": 128-wide Gauss-Jordan blocks and the Newton/QR
     products on the split-precision tensor-core GEMM; BASELINE bounds."""
