@@ -77,6 +77,9 @@ def parse():
     ap.add_argument("--polar-n", type=int, default=8192)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-blocks", type=int, default=300)
+    ap.add_argument("--no-pullback", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--sweep-tensors", type=int, default=256)
     ap.add_argument("--workload", choices=["qr", "gemm"], default="qr",
                     help="gemm: time the split-precision product alone on --gemm-shapes")
     ap.add_argument("--gemm-shapes", type=str, default="16384x8192x128,128x8192x16384",
@@ -472,6 +475,10 @@ def run_gb300(args):
             out["polar"]["mixed_over_fp64"] = round(p64["ms"] / out["polar"]["ms"], 3)
     if not args.no_batched and not args.lean:
         out["batched"] = batched_measure(mak, args, dev)
+    if not args.no_pullback and not args.lean:
+        out["pullback"] = pullback_measure(mak, args, dev)
+    if not args.no_sweep and not args.lean:
+        out["orth_sweep"] = sweep_measure(mak, args, dev)
 
     if rank == 0 and not args.no_cpu_baseline and not args.lean:
         ms_, ns_ = (int(x) for x in args.cpu_sample.split("x"))
@@ -590,6 +597,97 @@ def batched_measure(mak, args, dev):
                    for s_, (W, P) in zip(srcs[:8] + srcs[-8:], outs[:8] + outs[-8:]))
         res[f"polar_{prec}"] = {"ms": round(ms, 3), "blocks_per_s": round(nb * 1e3 / ms, 1),
                                 "newton_iterations": 10, "max_back_err_sampled": back}
+    return res
+
+
+def _crandn(rng, m, n, dev):
+    import torch
+
+    x = rng.standard_normal((n, m)) + 1j * rng.standard_normal((n, m))
+    return torch.from_numpy(x).to(dev).t()
+
+
+def pullback_measure(mak, args, dev):
+    """Differentiation workload: ComplexF64 1024 x 512 iid complex Gaussian,
+    cotangents iid complex Gaussian; forward + pullback of qr_compact and of
+    left_polar, both precisions (device-resident, one timed repetition after
+    a warm-up each), and the relative difference of the mixed dA from the
+    native one."""
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(SEED + 21)
+    m, n = 1024, 512
+    A0 = _crandn(rng, m, n, dev)
+    dQ, dR = _crandn(rng, m, n, dev), _crandn(rng, n, n, dev)
+    dW, dP = _crandn(rng, m, n, dev), _crandn(rng, n, n, dev)
+    res = {"workload": "ComplexF64 1024x512 iid complex Gaussian, cotangents iid complex Gaussian"}
+    dAs = {}
+    for prec in ("native", "mixed"):
+        def qr_fb():
+            A = A0.clone()
+            Q, R = mak.qr_compact_(A, None, precision=prec)
+            dA = torch.zeros_like(A0)
+            mak.qr_pullback_(dA, A0, (Q, R), (dQ, dR), precision=prec)
+            return dA
+
+        def polar_fb():
+            A = A0.clone()
+            W, P = mak.left_polar_(A, None, None, precision=prec)
+            dA = torch.zeros_like(A0)
+            mak.left_polar_pullback_(dA, A0, (W, P), (dW, dP), precision=prec)
+            return dA
+
+        for name, fn in (("qr", qr_fb), ("polar", polar_fb)):
+            fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dA = fn()
+            torch.cuda.synchronize()
+            res[f"{name}_{prec}_ms"] = round((time.perf_counter() - t0) * 1e3, 3)
+            dAs[(name, prec)] = dA
+    for name in ("qr", "polar"):
+        d = dAs[(name, "mixed")] - dAs[(name, "native")]
+        res[f"{name}_mixed_vs_native_rel"] = float(torch.linalg.norm(d) /
+                                                  torch.linalg.norm(dAs[(name, "native")]))
+        res[f"{name}_mixed_over_native"] = round(res[f"{name}_native_ms"] /
+                                                 res[f"{name}_mixed_ms"], 3)
+    return res
+
+
+def sweep_measure(mak, args, dev):
+    """Orthogonalisation sweep of a matrix-product canonicalisation: N
+    ComplexF64 tensors of bond dimension 256 and physical dimension 4, each a
+    1024 x 256 matrix (iid complex Gaussian).  One step = left_orth via QR of
+    every tensor (batched) + the QR pullback of the loss sum real(tr(D^H Q))
+    (dQ = D, dR = 0) for every tensor + left_polar of every tensor (batched,
+    10 Newton iterations).  Wall-clock time per step on the host (the
+    pullbacks synchronize once each), both precisions."""
+    import numpy as np
+    import torch
+
+    rng = np.random.default_rng(SEED + 31)
+    N = args.sweep_tensors
+    As = [_crandn(rng, 1024, 256, dev) for _ in range(N)]
+    Ds = [_crandn(rng, 1024, 256, dev) for _ in range(N)]
+    flops_qr = N * qr_flops(1024, 256, True)
+    res = {"workload": f"{N} ComplexF64 1024x256 tensors: batched QR + QR pullbacks + batched "
+                       f"polar (10 Newton iterations)", "qr_gflop": round(flops_qr / 1e9, 1)}
+    for prec in ("native", "mixed"):
+        def step():
+            outs = mak.batched_qr_compact(As, precision=prec)
+            for A, (Q, R), D in zip(As, outs, Ds):
+                dA = torch.zeros_like(A)
+                mak.qr_pullback_(dA, A, (Q, R), (D, None), precision=prec)
+            mak.batched_left_polar(As, precision=prec, maxiter=10)
+
+        step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step()
+        torch.cuda.synchronize()
+        res[f"{prec}_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+    res["mixed_over_native"] = round(res["native_ms"] / res["mixed_ms"], 3)
     return res
 
 

@@ -161,6 +161,10 @@ static int batched(int kind, const mak_batch_item* items, int nitems, const void
   });
   int rc_all = 0;
   set_lookahead(false);  // the batch's streams already overlap the blocks
+  // a quarter of the SMs per split product, so that several blocks'
+  // persistent tensor-core grids and native kernels share the GPU
+  const int budget0 = split_gemm_cta_budget();
+  set_split_gemm_cta_budget(num_sms() / 4);
   for (int i : order) {
     const int s = p.owner[i];
     Arena ar((char*)work + p.off[s], p.ws_stream[s]);
@@ -169,6 +173,7 @@ static int batched(int kind, const mak_batch_item* items, int nitems, const void
     if (rc != 0 && rc_all == 0) rc_all = rc;
   }
   set_lookahead(true);
+  set_split_gemm_cta_budget(budget0);
   for (int s = 0; s < BATCH_STREAMS; s++) {
     MAK_CUDA_TRY(cudaEventRecord(sp.join[s], sp.s[s]));
     MAK_CUDA_TRY(cudaStreamWaitEvent(st, sp.join[s], 0));

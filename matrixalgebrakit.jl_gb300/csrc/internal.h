@@ -28,6 +28,13 @@ int info_reset(cudaStream_t st, mak_info* info);
 bool lookahead_enabled();
 void set_lookahead(bool on);
 
+// Default cap on the persistent split-GEMM grid for calls made from the
+// current thread (0: one CTA per SM).  The batched driver lowers it so that
+// the products of blocks on different streams run side by side instead of
+// one persistent grid holding every SM.
+int split_gemm_cta_budget();
+void set_split_gemm_cta_budget(int ctas);
+
 // Left polar decomposition by scaled Newton (W m x n, P n x n or nullptr);
 // tol < 0 selects the fixed-iteration, host-sync-free mode.
 template <class T>

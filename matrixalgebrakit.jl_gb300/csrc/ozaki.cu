@@ -687,9 +687,11 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> s, int R, int K,
                                                        int Kpad, const int* E,
                                                        __nv_bfloat16* planes) {
   __shared__ double tile[64][65];
+  __shared__ unsigned short lut[129];  // bf16 bits of the integers -64 .. 64
   const int r0 = blockIdx.y * 64, k0 = blockIdx.x * 64;
   const int tid = threadIdx.x;
   const bool cr = oz_contig_r(s);
+  if (tid < 129) lut[tid] = __bfloat16_as_ushort(__float2bfloat16_rn((float)(tid - 64)));
   for (int e = tid; e < 64 * 64; e += 256) {
     int rr, kk;
     if (cr) { rr = e % 64; kk = e / 64; } else { kk = e % 64; rr = e / 64; }
@@ -698,10 +700,13 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> s, int R, int K,
   }
   __syncthreads();
   constexpr int FB = OZ_BITS * S;  // fractional bits of the fixed-point value
-  constexpr long long DMASK = (1ll << OZ_BITS) - 1;
-  constexpr long long HALF = 1ll << (OZ_BITS - 1);
+  static_assert(FB <= 56, "the fixed-point value fits 28 + 28 bits");
   const size_t plane_stride = (size_t)Rpad * Kpad;
-  // each thread: one row, a pair of adjacent k
+  // each thread: one row, a pair of adjacent k.  Digits are cut with 32-bit
+  // integer operations (the value as two 28-bit halves) and each bf16 plane
+  // value d 2^(-7p) is assembled from a table of the bf16 bit patterns of the
+  // digits -64..64 by lowering the exponent field by 7p: no conversion
+  // instructions.
   for (int e = tid; e < 64 * 32; e += 256) {
     const int rr = e / 32, kp = (e % 32) * 2;
     const int r = r0 + rr;
@@ -711,45 +716,45 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> s, int R, int K,
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       const double x = tile[rr][kp + h];
-      const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-      const bool neg = (b >> 63) != 0;
-      int ex = (int)((b >> 52) & 0x7FF);
-      unsigned long long m = b & 0x000FFFFFFFFFFFFFull;
+      const unsigned long long bts = (unsigned long long)__double_as_longlong(x);
+      const bool neg = (bts >> 63) != 0;
+      int ex = (int)((bts >> 52) & 0x7FF);
+      unsigned long long m = bts & 0x000FFFFFFFFFFFFFull;
       if (ex == 0) ex = 1; else m |= 0x0010000000000000ull;
       // f = |x| 2^(FB - Fr) rounded to nearest: f <= 2^(FB - 1)
       const int sh = ex - 1075 + FB - Fr;
-      long long f;
-      if ((b & 0x7FFFFFFFFFFFFFFFull) == 0) f = 0;
-      else if (sh >= 0) f = (sh >= 11) ? 0 : (long long)(m << sh);
+      unsigned long long f;
+      if ((bts & 0x7FFFFFFFFFFFFFFFull) == 0) f = 0;
+      else if (sh >= 0) f = (sh >= 11) ? 0 : (m << sh);
       else if (-sh >= 55) f = 0;
-      else f = (long long)((m >> (-sh)) + ((m >> (-sh - 1)) & 1ull));
+      else f = (m >> (-sh)) + ((m >> (-sh - 1)) & 1ull);
       // balanced base-2^7 digits from the bottom: d_p in [-64, 63] for
-      // p >= 2, leading digit in [0, 64]
+      // p >= 1, leading digit in [0, 64]; the low 28-bit half holds the four
+      // lowest digits, the carry then continues into the high half
+      const int hi28 = (int)(f >> 28);
+      int cur = (int)(f & 0xFFFFFFFull);
 #pragma unroll
       for (int p = S - 1; p >= 1; p--) {
-        long long d = f & DMASK;
-        f >>= OZ_BITS;
-        if (d >= HALF) {
-          d -= DMASK + 1;
-          f += 1;
+        if (p == S - 5) cur += hi28;
+        int d = cur & 127;
+        cur >>= OZ_BITS;
+        if (d >= 64) {
+          d -= 128;
+          cur += 1;
         }
-        dig[h][p] = (int)d;
+        dig[h][p] = neg ? -d : d;
       }
-      dig[h][0] = (int)f;
-      if (neg) {
-#pragma unroll
-        for (int p = 0; p < S; p++) dig[h][p] = -dig[h][p];
-      }
+      dig[h][0] = neg ? -cur : cur;
     }
 #pragma unroll
     for (int p = 0; p < S; p++) {
-      const float sc = __int_as_float((127 - OZ_BITS * p) << 23);  // 2^(-7p)
-      __nv_bfloat162 v;
-      v.x = __float2bfloat16_rn((float)dig[0][p] * sc);
-      v.y = __float2bfloat16_rn((float)dig[1][p] * sc);
+      unsigned b0 = lut[dig[0][p] + 64], b1 = lut[dig[1][p] + 64];
+      b0 = (b0 & 0x7FFFu) ? b0 - (unsigned)(OZ_BITS * p << 7) : b0;
+      b1 = (b1 & 0x7FFFu) ? b1 - (unsigned)(OZ_BITS * p << 7) : b1;
       const int k = k0 + kp;
       if (k < Kpad)
-        *reinterpret_cast<__nv_bfloat162*>(planes + p * plane_stride + (size_t)r * Kpad + k) = v;
+        *reinterpret_cast<unsigned*>(planes + p * plane_stride + (size_t)r * Kpad + k) =
+            b0 | (b1 << 16);
     }
   }
 }
@@ -891,6 +896,7 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
                 (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_, part, part ? M * Nl : 0,
                 status};
     const int64_t nwork = (int64_t)tm * tn * splits;
+    if (max_ctas <= 0) max_ctas = split_gemm_cta_budget();
     const int cap = (max_ctas > 0 && max_ctas < num_sms()) ? max_ctas : num_sms();
     const int grid = (int)(nwork < cap ? nwork : cap);
     note_launch();

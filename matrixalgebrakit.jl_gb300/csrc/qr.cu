@@ -402,6 +402,9 @@ struct LookAhead {
 static thread_local bool tl_no_lookahead = false;
 bool lookahead_enabled() { return !tl_no_lookahead; }
 void set_lookahead(bool on) { tl_no_lookahead = !on; }
+static thread_local int tl_gemm_budget = 0;
+int split_gemm_cta_budget() { return tl_gemm_budget; }
+void set_split_gemm_cta_budget(int ctas) { tl_gemm_budget = ctas > 0 ? ctas : 0; }
 static LookAhead* lookahead() {
   static LookAhead la;
   static bool ok = false;
