@@ -107,6 +107,80 @@ template <class R> __device__ __forceinline__ cplx<R> sign_safe_(cplx<R> s) {
   return {s.re / a, s.im / a};
 }
 
+// Reciprocal and square root for the panels' scalars.  GB300 issues about
+// 1.6 FP64 operations per clock per SM, so a single thread's chain of
+// dependent FP64 operations advances slowly, and IEEE division / square root
+// sequences sit on every panel column's critical path.  Here both use the
+// Newton-Raphson iteration (quadratic convergence; e.g. J.-M. Muller et
+// al., Handbook of Floating-Point Arithmetic, ch. 5), seeded in single
+// precision: 1/x by y <- y + y (1 - x y), 1/sqrt(x) by y <- y (3 - x y^2) / 2,
+// then sqrt(x) = x y with one correction s <- s + (x - s^2) y / 2.  The
+// argument is first reduced to [1, 2) (reciprocal) or [1, 4) (square root)
+// by integer exponent arithmetic; |exponent| <= 1000 is required.
+__device__ __forceinline__ double rcp_nr(double x) {
+  const long long bits = __double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7FF) - 1023;
+  const double m = __longlong_as_double((bits & (long long)0x800FFFFFFFFFFFFFull) |
+                                        0x3FF0000000000000ll);
+  double y = (double)__frcp_rn((float)m);
+  double r = fma(-m, y, 1.0);
+  y = fma(y, r, y);
+  r = fma(-m, y, 1.0);
+  y = fma(y, r, y);
+  return __longlong_as_double(__double_as_longlong(y) - ((long long)e << 52));
+}
+__device__ __forceinline__ double sqrt_nr(double x) {
+  const long long bits = __double_as_longlong(x);
+  const int e = (int)((bits >> 52) & 0x7FF) - 1023;
+  const int k = e >> 1;  // floor(e / 2): x 2^-2k in [1, 4)
+  const double m = __longlong_as_double(bits - ((long long)(2 * k) << 52));
+  double y = (double)rsqrtf((float)m);
+  y = y * fma(-0.5 * m * y, y, 1.5);
+  y = y * fma(-0.5 * m * y, y, 1.5);
+  double s = m * y;
+  s = fma(fma(-s, s, m), 0.5 * y, s);
+  return __longlong_as_double(__double_as_longlong(s) + ((long long)k << 52));
+}
+__device__ __forceinline__ float rcp_nr(float x) { return 1.0f / x; }
+// sqrt of a non-negative sum of squares: the Newton form inside the normal
+// range, the IEEE square root for 0, subnormals, huge values, Inf and NaN
+__device__ __forceinline__ double sqrt_nr_safe(double x) {
+  const int e = (int)((__double_as_longlong(x) >> 52) & 0x7FF) - 1023;
+  return (x > 0.0 && e > -1000 && e < 1000) ? sqrt_nr(x) : sqrt(x);
+}
+__device__ __forceinline__ float sqrt_nr_safe(float x) { return sqrtf(x); }
+__device__ __forceinline__ float sqrt_nr(float x) { return sqrtf(x); }
+// exponent e of a positive finite x (x = f 2^e, f in [1, 2)); subnormals give -1023
+__device__ __forceinline__ int exp2_of(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7FF) - 1023;
+}
+__device__ __forceinline__ int exp2_of(float x) { return (int)((__float_as_uint(x) >> 23) & 0xFF) - 127; }
+__device__ __forceinline__ double pow2_(double, int e) { return __longlong_as_double((long long)(e + 1023) << 52); }
+__device__ __forceinline__ float pow2_(float, int e) { return __uint_as_float((unsigned)(e + 127) << 23); }
+
+// 1/x for the pivots and reflectors: the Newton form inside the normal
+// range, IEEE division outside it (0, subnormals, huge values, Inf, NaN)
+__device__ __forceinline__ double rcp_nr_safe(double x) {
+  const int e = (int)((__double_as_longlong(x) >> 52) & 0x7FF) - 1023;
+  return (e > -1000 && e < 1000) ? rcp_nr(x) : 1.0 / x;
+}
+__device__ __forceinline__ float rcp_nr_safe(float x) { return 1.0f / x; }
+// 1/z for real and complex scalars (complex: conj(z) / |z|^2 with the
+// components scaled by a power of two near |z|)
+__device__ __forceinline__ double inv_fast(double x) { return rcp_nr_safe(x); }
+__device__ __forceinline__ float inv_fast(float x) { return 1.0f / x; }
+template <class R> __device__ __forceinline__ cplx<R> inv_fast(cplx<R> z) {
+  const R w = fmax(fabs(z.re), fabs(z.im));
+  if (!(w > R(0)) || !(w < R(INFINITY))) return inv_(z);
+  const int e = exp2_of(w);
+  const int lim = sizeof(R) == 8 ? 1000 : 100;
+  if (e < -lim || e > lim) return inv_(z);
+  const R sd = pow2_(R(0), -e);
+  const R z1 = z.re * sd, z2 = z.im * sd;
+  const R d = rcp_nr(fma_(z1, z1, z2 * z2)) * sd;
+  return {z1 * d, -z2 * d};
+}
+
 // L1-bypassing loads for values written by other CTAs of the same launch
 // (after a grid barrier); L1 is not coherent across SMs.
 __device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
   __shared__ int si[32];
   __shared__ T prow[GJ_NB];
   __shared__ T srow[GJ_NB];
+  __shared__ T dinv_s;
   __shared__ int pivs;
   const int G = gridDim.x, cb = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
@@ -130,11 +131,13 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
     if (p != jj && p >= r0 && p < r0 + nr)
       for (int c = tid; c < b; c += blockDim.x) Ps[(p - r0) + c * rpc] = ld_cg(&a.swapbuf[c]);
     __syncthreads();
-    const T d = prow[j];
-    if (d == zero_<T>()) {
-      if (tid == 0) atomicExch(a.singular, 1);
+    if (tid == 0) {
+      const T d = prow[j];
+      if (d == zero_<T>()) atomicExch(a.singular, 1);
+      dinv_s = inv_fast(d);  // once per column: a dependent FP64 chain
     }
-    const T dinv = inv_(d);
+    __syncthreads();
+    const T dinv = dinv_s;
     // the scaled pivot row, formed once (GB300 issues about 1.6 FP64
     // operations per clock per SM, so the elimination keeps one FMA per
     // element); its own column holds the new pivot-column entry 1/d

@@ -47,9 +47,10 @@ struct PanelArgs {
   T* tau;               // [jb]
   T* Tm;                // [NBMAX x NBMAX], ld NBMAX
   real_t<T>* part_nrm;  // [3][gstride]: sums of squares, largest magnitudes, rescaled sums
-  T* part_w;            // [G][NBMAX]
+  T* part_w;            // [G][NBMAX]: w partials, one row of NBMAX columns per CTA
   T* part_g;            // [G][NBMAX*NBMAX]
   T* alpha_buf;         // [NBMAX]
+  T* gram;              // [NBMAX*NBMAX]: the panel's reduced Gram matrix V^H V
   unsigned* bar;        // grid barrier words
   int* status;
   int gstride;          // allocation stride of the per-CTA partial rows
@@ -114,6 +115,9 @@ template <class R> __device__ __forceinline__ int norm_needs_rescale(typename No
 
 // beta / tau / 1/(alpha-beta) of one reflector, LAPACK ?larfg convention:
 // H^H [alpha; x] = [beta; 0], H = I - tau v v^H, v = [1; x/(alpha-beta)].
+// One reciprocal of beta, one of alpha - beta (|.|^2 for complex) and one
+// square root; values are scaled by exact powers of two, and magnitudes near
+// the ends of the exponent range take the IEEE operations.
 template <class T>
 __device__ void larfg_scalars(T alpha, real_t<T> xnorm, T& beta, T& tau, T& scal) {
   using R = real_t<T>;
@@ -124,12 +128,33 @@ __device__ void larfg_scalars(T alpha, real_t<T> xnorm, T& beta, T& tau, T& scal
     scal = one_<T>();
     return;
   }
-  R w = fmax(fmax(fabs(ar), fabs(ai)), xnorm);
-  R nrm = w * sqrt((ar / w) * (ar / w) + (ai / w) * (ai / w) + (xnorm / w) * (xnorm / w));
-  R b = ar >= R(0) ? -nrm : nrm;
+  const R w = fmax(fmax(fabs(ar), fabs(ai)), xnorm);
+  const int ew = exp2_of(w);
+  const int lim = sizeof(R) == 8 ? 1000 : 100;
+  if (ew < -lim + 4 || ew > lim - 4) {
+    R nrm = w * sqrt((ar / w) * (ar / w) + (ai / w) * (ai / w) + (xnorm / w) * (xnorm / w));
+    R b = ar >= R(0) ? -nrm : nrm;
+    beta = make_scalar<T>(b, 0);
+    tau = make_scalar<T>((b - ar) / b, -ai / b);
+    scal = inv_(alpha - beta);
+    return;
+  }
+  const R sd = pow2_(R(0), -ew), su = pow2_(R(0), ew);  // exact scalings
+  const R a1 = ar * sd, a2 = ai * sd, a3 = xnorm * sd;
+  const R nrm = sqrt_nr(fma_(a1, a1, fma_(a2, a2, a3 * a3))) * su;
+  const R b = ar >= R(0) ? -nrm : nrm;
+  const R rb = rcp_nr(b);
   beta = make_scalar<T>(b, 0);
-  tau = make_scalar<T>((b - ar) / b, -ai / b);
-  scal = inv_(alpha - beta);
+  tau = make_scalar<T>((b - ar) * rb, -ai * rb);
+  // alpha - beta = (ar - b, ai) with |ar - b| = |ar| + nrm >= nrm
+  const R zr = ar - b;
+  if constexpr (traits<T>::cpx) {
+    const R z1 = zr * sd, z2 = ai * sd;  // |z| in [2^-1, 4) after scaling by w
+    const R d = rcp_nr(fma_(z1, z1, z2 * z2)) * sd;
+    scal = make_scalar<T>(z1 * d, -z2 * d);
+  } else {
+    scal = make_scalar<T>(rcp_nr(zr), 0);
+  }
 }
 
 template <class T>
@@ -142,6 +167,7 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
   __shared__ R sc_r[3];
   __shared__ int sc_flag;
   __shared__ T wsh[NBMAX];
+  __shared__ T red_w[PANEL_THREADS / 32][NBMAX];
   __shared__ T sc[3];
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
@@ -208,7 +234,7 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
       }
     }
     __syncthreads();
-    R xnorm = sqrt(sc_r[0]);
+    R xnorm = R(0);  // meaningful in thread 0 only (the scalars below)
     if (sc_flag) {
       // rare: rescale by 2^-e, e the exponent of the largest magnitude
       // (clamped so the scale itself stays finite), then sum again
@@ -231,6 +257,7 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
       xnorm = sc_r[2];
     }
     if (tid == 0) {
+      if (!sc_flag) xnorm = sqrt_nr_safe(sc_r[0]);
       T alpha = ld_cg(&a.alpha_buf[j]);
       T beta, tau, scal;
       larfg_scalars(alpha, xnorm, beta, tau, scal);
@@ -255,33 +282,31 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
         s = fma_(conj_(v), Ps[r + c * rpc], s);
       }
       s = warp_sum(s);
-      if (lane == 0) a.part_w[(int64_t)c * a.gstride + b] = s;
+      if (lane == 0) a.part_w[(int64_t)b * NBMAX + c] = s;
     }
     if (!grid_barrier(a.bar, G, a.status)) return;
 
-    // ---- phase C: combine w in a fixed order (coalesced partial rows, all
-    // loads of a warp issued before its reductions), apply H_j^H to columns > j
+    // ---- phase C: combine w in a fixed order: lane = column, warp w sums
+    // the partials of a slice of the CTAs (coalesced rows of part_w), then
+    // warp 0 adds the slices; every CTA gets bit-identical w
     {
-      constexpr int CPW = (NBMAX + 7) / 8;  // columns per warp with 8 warps
-      T acc_c[CPW];
-#pragma unroll
-      for (int i = 0; i < CPW; i++) {
-        acc_c[i] = zero_<T>();
-        const int c = j + 1 + wid + i * nw;
-        if (c < jb)
-          for (int q = lane; q < G; q += 32) acc_c[i] += ld_cg(&a.part_w[(int64_t)c * a.gstride + q]);
-      }
-#pragma unroll
-      for (int i = 0; i < CPW; i++) {
-        const int c = j + 1 + wid + i * nw;
-        T s = warp_sum(acc_c[i]);
-        if (lane == 0 && c < jb) wsh[c] = s;
-      }
+      const int per = (G + nw - 1) / nw;
+      const int q0 = wid * per, q1 = min(G, q0 + per);
+      T acc = zero_<T>();
+      if (lane > j && lane < jb)
+        for (int q = q0; q < q1; q++) acc += ld_cg(&a.part_w[(int64_t)q * NBMAX + lane]);
+      red_w[wid][lane] = acc;
     }
     __syncthreads();
-    const T ctau = conj_(tau);
+    if (wid == 0) {
+      T sum = zero_<T>();
+      for (int w = 0; w < nw; w++) sum += red_w[w][lane];
+      // the update's coefficient f_c = conj(tau) w_c, formed once per column
+      if (lane > j && lane < jb) wsh[lane] = conj_(tau) * sum;
+    }
+    __syncthreads();
     for (int c = j + 1; c < jb; c++) {
-      const T f = ctau * wsh[c];
+      const T f = wsh[c];
       T* pc = Ps + c * rpc;
       for (int r = rj + tid; r < nr; r += blockDim.x) {
         T v = (r0 + r == j) ? one_<T>() : col[r];
@@ -291,54 +316,64 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
     __syncthreads();
   }
 
-  // ---- Gram partials of V (unit lower trapezoidal) for the T factor
-  for (int pr = wid; pr < jb * jb; pr += nw) {
-    const int i = pr % jb, jj = pr / jb;
-    if (i >= jj) continue;
-    T s = zero_<T>();
-    const int rb = max(0, i - r0);
-    for (int r = rb + lane; r < nr; r += 32) {
-      const int gr = r0 + r;
-      T vi = (gr == i) ? one_<T>() : Ps[r + i * rpc];
-      T vj = (gr == jj) ? one_<T>() : (gr > jj ? Ps[r + jj * rpc] : zero_<T>());
-      s = fma_(conj_(vi), vj, s);
+  // ---- Gram partials of V (unit lower trapezoidal) for the T factor: one
+  // thread per pair (i, jj), i < jj, over this CTA's rows (no reductions)
+  const int npairs = jb * (jb - 1) / 2;
+  for (int pq = tid; pq < npairs; pq += blockDim.x) {
+    int jj = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)pq)) * 0.5f);
+    while (jj * (jj - 1) / 2 > pq) jj--;
+    while (jj * (jj + 1) / 2 <= pq) jj++;
+    const int i = pq - jj * (jj - 1) / 2;
+    T s0 = zero_<T>(), s1 = zero_<T>();
+    const int rb = max(0, jj - r0);
+    int r = rb;
+    if (r < nr && r0 + r == jj) {  // v_jj = 1 on its diagonal row
+      s0 = conj_(Ps[r + i * rpc]);
+      r++;
     }
-    s = warp_sum(s);
-    if (lane == 0) a.part_g[(int64_t)b * NBMAX * NBMAX + i + jj * NBMAX] = s;
+    for (; r + 1 < nr; r += 2) {
+      s0 = fma_(conj_(Ps[r + i * rpc]), Ps[r + jj * rpc], s0);
+      s1 = fma_(conj_(Ps[r + 1 + i * rpc]), Ps[r + 1 + jj * rpc], s1);
+    }
+    if (r < nr) s0 = fma_(conj_(Ps[r + i * rpc]), Ps[r + jj * rpc], s0);
+    a.part_g[(int64_t)b * NBMAX * NBMAX + i + jj * NBMAX] = s0 + s1;
   }
   for (int c = 0; c < jb; c++)
     for (int r = tid; r < nr; r += blockDim.x) a.A[(r0 + r) + (int64_t)c * a.lda] = Ps[r + c * rpc];
   if (!grid_barrier(a.bar, G, a.status)) return;
-  if (b != 0) return;
 
-  // ---- CTA 0: T factor, larft forward column-wise recurrence
-  __shared__ T gram[NBMAX][NBMAX + 1];
-  __shared__ T tt[NBMAX][NBMAX + 1];
-  __shared__ T tv[NBMAX];
-  for (int pr = tid; pr < jb * jb; pr += blockDim.x) {
-    const int i = pr % jb, jj = pr / jb;
+  // ---- reduce the Gram over the CTAs: one warp per pair, lanes over the
+  // CTAs' partials, fixed order
+  for (int pq = b * nw + wid; pq < npairs; pq += G * nw) {
+    int jj = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)pq)) * 0.5f);
+    while (jj * (jj - 1) / 2 > pq) jj--;
+    while (jj * (jj + 1) / 2 <= pq) jj++;
+    const int i = pq - jj * (jj - 1) / 2;
     T s = zero_<T>();
-    if (i < jj)
-      for (int q = 0; q < G; q++) s += ld_cg(&a.part_g[(int64_t)q * NBMAX * NBMAX + i + jj * NBMAX]);
-    gram[i][jj] = s;
-    tt[i][jj] = zero_<T>();
+    for (int q = lane; q < G; q += 32) s += ld_cg(&a.part_g[(int64_t)q * NBMAX * NBMAX + i + jj * NBMAX]);
+    s = warp_sum(s);
+    if (lane == 0) a.gram[i + jj * NBMAX] = s;
   }
-  __syncthreads();
-  for (int jj = 0; jj < jb; jj++) {
-    const T tj = a.tau[jj];
-    if (tid < jj) tv[tid] = -(tj * gram[tid][jj]);
-    __syncthreads();
-    if (tid < jj) {
-      T s = zero_<T>();
-      for (int l = tid; l < jj; l++) s = fma_(tt[tid][l], tv[l], s);
-      tt[tid][jj] = s;
+  if (!grid_barrier(a.bar, G, a.status)) return;
+
+  // ---- T factor (larft, forward, column-wise): T = U^{-1} with U_ii =
+  // 1/tau_i and U_il = G_il (i < l), each column an independent back
+  // substitution x_k = tau_k, x_i = -tau_i sum_{l=i+1..k} G_il x_l (tau_i as
+  // a factor: tau_i = 0 needs no division).  Warp 0 of CTA c computes
+  // columns c, c + G, ...; lane i owns row i.
+  if (wid != 0) return;
+  for (int k = b; k < NBMAX; k += G) {
+    T x = zero_<T>();
+    if (k < jb) {
+      T acc = zero_<T>();
+      for (int l = k; l >= 0; l--) {
+        const T mine = (l == k) ? ld_cg(&a.tau[k]) : -(ld_cg(&a.tau[l]) * acc);
+        const T xl = shfl_idx_(mine, l);
+        if (lane == l) x = xl;
+        if (lane < l) acc = fma_(ld_cg(&a.gram[lane + l * NBMAX]), xl, acc);
+      }
     }
-    if (tid == 0) tt[jj][jj] = tj;
-    __syncthreads();
-  }
-  for (int pr = tid; pr < NBMAX * NBMAX; pr += blockDim.x) {
-    const int i = pr % NBMAX, jj = pr / NBMAX;
-    a.Tm[i + jj * NBMAX] = (i < jb && jj < jb) ? tt[i][jj] : zero_<T>();
+    a.Tm[lane + k * NBMAX] = (k < jb && lane <= k) ? x : zero_<T>();
   }
 }
 
@@ -626,6 +661,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   T* part_w = ar.take<T>((size_t)gmax * NBMAX);
   T* part_g = ar.take<T>((size_t)gmax * NBMAX * NBMAX);
   T* alpha_buf = ar.take<T>(NBMAX);
+  T* gram_buf = ar.take<T>((size_t)NBMAX * NBMAX);
   unsigned* bar = ar.take<unsigned>(2);
   T *To = nullptr, *Gm = nullptr, *Wm = nullptr, *W2m = nullptr;
   char* ozs = nullptr;
@@ -712,8 +748,8 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     PanelShape ps;
     MAK_TRY(panel_shape<T>(mp, jb, ps, s == st ? sms : lookahead_ctas()));
     PanelArgs<T> pa{A + j0 + j0 * lda, lda, (int)mp, jb, ps.rpc, tau + j0,
-                    Ts + (j0 / nb) * NBMAX * NBMAX, part_nrm, part_w, part_g, alpha_buf, bar,
-                    status, gmax};
+                    Ts + (j0 / nb) * NBMAX * NBMAX, part_nrm, part_w, part_g, alpha_buf,
+                    gram_buf, bar, status, gmax};
     void* args[] = {&pa};
     ProfScope prof(s, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
     note_launch();
