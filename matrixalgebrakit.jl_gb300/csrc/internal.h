@@ -24,9 +24,20 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
 
 int info_reset(cudaStream_t st, mak_info* info);
 
-// QR look-ahead (side stream) on/off for calls made from the current thread
+// Look-ahead (QR and Gauss-Jordan): a high-priority side stream factors the
+// next block while the main stream updates the far columns.  On/off for
+// calls made from the current thread; the side stream and its events belong
+// to the calling thread (nullptr if they could not be created); the side
+// stream's kernels use lookahead_ctas() SMs and the main stream's persistent
+// tensor-core grid the rest.
 bool lookahead_enabled();
 void set_lookahead(bool on);
+struct LookAhead {
+  cudaStream_t side;
+  cudaEvent_t ev_ready, ev_done;
+};
+LookAhead* lookahead();
+int lookahead_ctas();
 
 // Default cap on the persistent split-GEMM grid for calls made from the
 // current thread (0: one CTA per SM).  The batched driver lowers it so that

@@ -264,16 +264,18 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
   note_launch();
   iota_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>((int)n, piv);
   const size_t cap = gj_slab_cap<T>();
-  for (int64_t k0 = 0; k0 < n; k0 += GJ_NB) {
-    const int b = (int)((n - k0) < GJ_NB ? (n - k0) : GJ_NB);
-    const int64_t K0 = (k0 / NBO) * NBO;  // enclosing block column
-    const int64_t KB = (n - K0) < NBO ? (n - K0) : NBO;
-    const int64_t c_lo = mixed ? K0 : 0, c_hi = mixed ? K0 + KB : n;
-    // grid: rows per CTA >= 64, one CTA per SM, slab within shared memory
+  // one 32-wide panel (cooperative launch, at most max_ctas CTAs: on the
+  // look-ahead side stream it leaves the other SMs to the main stream)
+  auto panel = [&](int64_t k0, int b, cudaStream_t s, int max_ctas) -> int {
+    // grid: rows per CTA >= 64, at most one CTA per SM, slab within shared memory
     int64_t G = ceil_div(n, 64);
-    if (G > sms) G = sms;
+    if (G > max_ctas) G = max_ctas;
     int64_t rpc = ceil_div(n, G);
-    if ((size_t)rpc * b * sizeof(T) > cap) return MAK_ERR_UNSUPPORTED;
+    if ((size_t)rpc * b * sizeof(T) > cap) {
+      G = ceil_div(n, (int64_t)(cap / ((size_t)b * sizeof(T))));
+      if (G > sms) return MAK_ERR_UNSUPPORTED;
+      rpc = ceil_div(n, G);
+    }
     G = ceil_div(n, rpc);
     size_t smem = (size_t)rpc * b * sizeof(T);
     int per_sm = 0;
@@ -284,40 +286,89 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
     GjArgs<T> ga{X, ldx, (int)n, (int)k0, b, (int)rpc, piv, part_val, part_idx, swapbuf,
                  bar, &info->status, &info->singular};
     void* args[] = {&ga};
-    {
-      ProfScope prof(st, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
-      note_launch();
-      MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)gje_panel_kernel<T>, dim3((unsigned)G),
-                                               dim3(GJ_THREADS), args, smem, st));
-    }
+    ProfScope prof(s, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
     note_launch();
-    gje_laswp_save_kernel<T><<<(unsigned)ceil_div(c_hi - c_lo, 128), 128, 0, st>>>(
-        (int)n, X, ldx, (int)k0, b, piv, buf, (int)c_lo, (int)c_hi);
-    MAK_CUDA_TRY(cudaGetLastError());
-    const T* F = X + k0 * ldx;
-    if (k0 > c_lo)
-      MAK_TRY(gemm<T>(st, n, k0 - c_lo, b, one_<T>(), opnd<T>(F, ldx),
-                      opnd<T>(buf + c_lo * b, b), one_<T>(), X + c_lo * ldx, ldx));
-    if (k0 + b < c_hi)
-      MAK_TRY(gemm<T>(st, n, c_hi - k0 - b, b, one_<T>(), opnd<T>(F, ldx),
-                      opnd<T>(buf + (k0 + b) * b, b), one_<T>(), X + (k0 + b) * ldx, ldx));
-    if (mixed && k0 + b == K0 + KB) {
-      // block column finished: exchanges + rank-KB update of the other columns
+    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)gje_panel_kernel<T>, dim3((unsigned)G),
+                                             dim3(GJ_THREADS), args, smem, s));
+    return 0;
+  };
+  // the panels of block column [K0, K0 + KB) with their updates confined to
+  // the block's columns (the whole elimination when not mixed: KB = n)
+  auto factor_block = [&](int64_t K0, int64_t KB, cudaStream_t s, int max_ctas) -> int {
+    const int64_t c_lo = K0, c_hi = K0 + KB;
+    for (int64_t k0 = K0; k0 < K0 + KB; k0 += GJ_NB) {
+      const int b = (int)((K0 + KB - k0) < GJ_NB ? (K0 + KB - k0) : GJ_NB);
+      MAK_TRY(panel(k0, b, s, max_ctas));
       note_launch();
-      gje_laswp_save_kernel<T><<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(
-          (int)n, X, ldx, (int)K0, (int)KB, piv, bufo, 0, (int)n);
+      gje_laswp_save_kernel<T><<<(unsigned)ceil_div(c_hi - c_lo, 128), 128, 0, s>>>(
+          (int)n, X, ldx, (int)k0, b, piv, buf, (int)c_lo, (int)c_hi);
       MAK_CUDA_TRY(cudaGetLastError());
-      const T* Fb = X + K0 * ldx;
-      if (K0 > 0) {
-        Arena oz(ozs, oz_bytes);
-        MAK_TRY(gemm_prec<T>(st, precision, n, K0, KB, one_<T>(), opnd<T>(Fb, ldx),
-                             opnd<T>(bufo, KB), one_<T>(), X, ldx, oz, &info->status));
-      }
-      if (K0 + KB < n) {
-        Arena oz(ozs, oz_bytes);
-        MAK_TRY(gemm_prec<T>(st, precision, n, n - K0 - KB, KB, one_<T>(), opnd<T>(Fb, ldx),
-                             opnd<T>(bufo + (K0 + KB) * KB, KB), one_<T>(),
-                             X + (K0 + KB) * ldx, ldx, oz, &info->status));
+      const T* F = X + k0 * ldx;
+      if (k0 > c_lo)
+        MAK_TRY(gemm<T>(s, n, k0 - c_lo, b, one_<T>(), opnd<T>(F, ldx),
+                        opnd<T>(buf + c_lo * b, b), one_<T>(), X + c_lo * ldx, ldx));
+      if (k0 + b < c_hi)
+        MAK_TRY(gemm<T>(s, n, c_hi - k0 - b, b, one_<T>(), opnd<T>(F, ldx),
+                        opnd<T>(buf + (k0 + b) * b, b), one_<T>(), X + (k0 + b) * ldx, ldx));
+    }
+    return 0;
+  };
+  // block column [K0, K0 + KB) applied to the columns [c_lo, c_hi) outside
+  // it: its row exchanges, then one rank-KB update (split-precision product)
+  auto apply_block = [&](int64_t K0, int64_t KB, int64_t c_lo, int64_t c_hi, cudaStream_t s,
+                         int max_ctas) -> int {
+    if (c_hi <= c_lo) return 0;
+    note_launch();
+    gje_laswp_save_kernel<T><<<(unsigned)ceil_div(c_hi - c_lo, 128), 128, 0, s>>>(
+        (int)n, X, ldx, (int)K0, (int)KB, piv, bufo, (int)c_lo, (int)c_hi);
+    MAK_CUDA_TRY(cudaGetLastError());
+    const T* Fb = X + K0 * ldx;
+    const int64_t l1 = c_hi < K0 ? c_hi : K0;  // left part [c_lo, l1)
+    if (l1 > c_lo) {
+      Arena oz(ozs, oz_bytes);
+      MAK_TRY(gemm_prec<T>(s, precision, n, l1 - c_lo, KB, one_<T>(), opnd<T>(Fb, ldx),
+                           opnd<T>(bufo + c_lo * KB, KB), one_<T>(), X + c_lo * ldx, ldx, oz,
+                           &info->status, max_ctas));
+    }
+    const int64_t r0 = c_lo > K0 + KB ? c_lo : K0 + KB;  // right part [r0, c_hi)
+    if (c_hi > r0) {
+      Arena oz(ozs, oz_bytes);
+      MAK_TRY(gemm_prec<T>(s, precision, n, c_hi - r0, KB, one_<T>(), opnd<T>(Fb, ldx),
+                           opnd<T>(bufo + r0 * KB, KB), one_<T>(), X + r0 * ldx, ldx, oz,
+                           &info->status, max_ctas));
+    }
+    return 0;
+  };
+
+  if (!mixed) {
+    MAK_TRY(factor_block(0, n, st, sms));
+  } else {
+    // Look-ahead: block K is applied first to block K+1's columns; the side
+    // stream then factors block K+1 (its panels touch only its own columns,
+    // and its row exchanges reach the other columns when block K+1 is
+    // applied) while the main stream applies block K to the remaining
+    // columns.
+    const int64_t nblk = ceil_div(n, (int64_t)NBO);
+    LookAhead* la = (nblk > 1 && lookahead_enabled() && n >= 2048) ? lookahead() : nullptr;
+    const int la_ctas = lookahead_ctas();
+    MAK_TRY(factor_block(0, n < NBO ? n : NBO, st, sms));
+    for (int64_t K = 0; K < nblk; K++) {
+      const int64_t K0 = K * NBO, KB = (n - K0) < NBO ? (n - K0) : NBO;
+      const int64_t nx = K0 + KB;
+      const bool has_next = nx < n;
+      const int64_t nKB = has_next ? ((n - nx) < NBO ? (n - nx) : NBO) : 0;
+      if (has_next && la) {
+        MAK_TRY(apply_block(K0, KB, nx, nx + nKB, st, 0));
+        MAK_CUDA_TRY(cudaEventRecord(la->ev_ready, st));
+        MAK_CUDA_TRY(cudaStreamWaitEvent(la->side, la->ev_ready, 0));
+        MAK_TRY(factor_block(nx, nKB, la->side, la_ctas));
+        MAK_CUDA_TRY(cudaEventRecord(la->ev_done, la->side));
+        MAK_TRY(apply_block(K0, KB, 0, K0, st, sms - la_ctas));
+        MAK_TRY(apply_block(K0, KB, nx + nKB, n, st, sms - la_ctas));
+        MAK_CUDA_TRY(cudaStreamWaitEvent(st, la->ev_done, 0));
+      } else {
+        MAK_TRY(apply_block(K0, KB, 0, n, st, 0));
+        if (has_next) MAK_TRY(factor_block(nx, nKB, st, sms));
       }
     }
   }

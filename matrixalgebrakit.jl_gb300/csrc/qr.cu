@@ -413,7 +413,7 @@ constexpr int QR_OUTER_NB = 128;  // outer block of the mixed-precision path
 // SMs given to the look-ahead side stream (panels and the block Gram) while
 // the main stream's persistent tensor-core grid takes the rest; 48 by
 // default, MAK_LOOKAHEAD_CTAS overrides it (read once, clamped to 8..120).
-static int lookahead_ctas() {
+int lookahead_ctas() {
   static int v = 48;
   static std::once_flag f;
   std::call_once(f, [] {
@@ -426,32 +426,31 @@ static int lookahead_ctas() {
   return v;
 }
 
-// Side stream (highest priority, so its panel CTAs are scheduled ahead of
-// the trailing GEMM's) and events of the look-ahead; created once, on first
-// use (before any graph capture).  Calls issued from the batched driver run
-// without look-ahead (lookahead_enabled() is false on that thread).
-struct LookAhead {
-  cudaStream_t side;
-  cudaEvent_t ev_ready, ev_done;
-};
 static thread_local bool tl_no_lookahead = false;
 bool lookahead_enabled() { return !tl_no_lookahead; }
 void set_lookahead(bool on) { tl_no_lookahead = !on; }
 static thread_local int tl_gemm_budget = 0;
 int split_gemm_cta_budget() { return tl_gemm_budget; }
 void set_split_gemm_cta_budget(int ctas) { tl_gemm_budget = ctas > 0 ? ctas : 0; }
-static LookAhead* lookahead() {
-  static LookAhead la;
-  static bool ok = false;
-  static std::once_flag f;
-  std::call_once(f, [] {
+
+// Side stream (highest priority, so its panel CTAs are scheduled ahead of
+// the trailing GEMM's) and events of the look-ahead, one set per host
+// thread so that calls from several threads never share an event; created
+// on the thread's first large call (which must precede any graph capture on
+// that thread).
+LookAhead* lookahead() {
+  static thread_local LookAhead la;
+  static thread_local int state = 0;  // 0 not created, 1 ready, -1 failed
+  if (state == 0) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    ok = cudaStreamCreateWithPriority(&la.side, cudaStreamNonBlocking, hi) == cudaSuccess &&
-         cudaEventCreateWithFlags(&la.ev_ready, cudaEventDisableTiming) == cudaSuccess &&
-         cudaEventCreateWithFlags(&la.ev_done, cudaEventDisableTiming) == cudaSuccess;
-  });
-  return ok ? &la : nullptr;
+    state = (cudaStreamCreateWithPriority(&la.side, cudaStreamNonBlocking, hi) == cudaSuccess &&
+             cudaEventCreateWithFlags(&la.ev_ready, cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&la.ev_done, cudaEventDisableTiming) == cudaSuccess)
+                ? 1
+                : -1;
+  }
+  return state == 1 ? &la : nullptr;
 }
 
 // T factor of a JB-wide block reflector (LAPACK larft, forward, column-wise

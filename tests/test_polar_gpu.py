@@ -127,3 +127,24 @@ def test_left_polar_mixed(mak, cuda, dt, shape):
     assert O.orth_error(Wh) <= 1e-12 * np.sqrt(shape[1])
     Wo, Po, _ = O.left_polar_newton(A)
     assert O.rel_err(Wh, Wo) <= 1e-8 and O.rel_err(Ph, Po) <= 1e-8
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128], ids=lambda d: np.dtype(d).name)
+def test_left_polar_mixed_lookahead(mak, cuda, dt):
+    """n >= 2048 in mixed precision: the Gauss-Jordan inverse factors block
+    column K+1 on the look-ahead side stream while block K updates the other
+    columns.  A = U diag(s) V^H with known polar factors W = U V^H and
+    P = V diag(s) V^H (s log-spaced 1 .. 1e-6)."""
+    rng = np.random.default_rng(29)
+    n = 2304
+    U, V = O.haar(rng, n, dt), O.haar(rng, n, dt)
+    s = np.logspace(0, -6, n)
+    A = np.asfortranarray(((U * s[None, :]) @ V.conj().T).astype(dt))
+    info = {}
+    W, P = mak.left_polar_(to_dev(A, cuda), None, None, precision="mixed", _info=info)
+    Wh, Ph = to_host(W), to_host(P)
+    assert info["converged"]
+    assert back_err(A, Wh, Ph) <= 1e-12
+    assert O.orth_error(Wh) <= 1e-12 * np.sqrt(n)
+    assert O.rel_err(Wh, U @ V.conj().T) <= 1e-8
+    assert O.rel_err(Ph, (V * s[None, :]) @ V.conj().T) <= 1e-8
