@@ -49,10 +49,16 @@ METRIC = ("QR/polar TFLOP/s + batched solves/s, mixed vs FP64 at "
           "‖A−QR‖/‖A‖≤1e-12")
 SEED = 20260101
 OZ_PAIRS = 36  # bf16 plane products per FP64 product in the split GEMM (8 slices)
-# DRAM traffic of the split GEMM per launch, from one ncu capture of the
-# bench workload (dram__bytes_read.sum + dram__bytes_write.sum, averaged over
-# the launches of one factorization; summary in profiles/)
-OZ_TRAFFIC = None
+# DRAM traffic of the split GEMM per FP64-equivalent flop, from ncu captures of
+# its two trailing-update shapes (dram__bytes_read.sum + dram__bytes_write.sum:
+# 0.059 B/flop for C -= V W2 with K = 128, 0.066 B/flop for W = V^H C with
+# K = 8192; summary in profiles/oz_gemm_kernel_trailing_update_shapes.md).
+# Both grow in proportion to the work, so the per-launch traffic is this
+# rate times the launch's FP64-equivalent flops.
+OZ_TRAFFIC = {"bytes_per_fp64_flop": 0.0626,
+              "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of oz_gemm_kernel on "
+                        "8192x4096x128 and 128x4096x8192 (bench.py --workload gemm), scaled by "
+                        "the launch's FP64-equivalent flops"}
 
 
 def parse():
@@ -389,7 +395,9 @@ def run_gb300(args):
     roofline = {"bound": "tensor", "achieved": round(achieved, 4),
                 "peak": round(peak, 4) if peak else None,
                 "unit": "TFLOP/s", "frac": round(achieved / peak, 4) if peak else None,
-                "traffic": traffic["bytes_per_launch"] if traffic else None,
+                "traffic": round(traffic["bytes_per_fp64_flop"] * g_work / max(1, g_cnt))
+                if traffic else None,
+                "traffic_unit": "bytes per launch",
                 "traffic_source": traffic["source"] if traffic else None,
                 "fp64_equivalent_tflops": round(fp64_equiv, 4),
                 "kernel": "gemm_kernel<double> (larfb / orgqr products)" if not mixed
@@ -785,7 +793,7 @@ def run_gemm(args):
         k_ms, k_work, k_cnt = _read_prof(lib, 1)
         f64 = 2.0 * m * n * k / (ms / 1e3) / 1e12
         kern = k_work / (k_ms / 1e3) / 1e12 if k_ms > 0 else None
-        out["shapes"].append({"m": m, "n": n, "k": k, "op_a": "CNT"[opA], "ms": round(ms, 4),
+        out["shapes"].append({"m": m, "n": n, "k": k, "op_a": "NTC"[opA], "ms": round(ms, 4),
                               "fp64_equiv_tflops": round(f64, 3),
                               "kernel_ms": round(k_ms / max(1, k_cnt), 4),
                               "kernel_fp64_equiv_tflops": round(kern, 3) if kern else None,

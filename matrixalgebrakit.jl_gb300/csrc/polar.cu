@@ -232,11 +232,14 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
   // mixed precision: 128-wide block columns, eliminated with 32-wide panels
   // whose updates stay inside the block; the other columns then receive one
   // rank-128 update through the split-precision tensor-core GEMM
-  // as in the QR: the 128-wide blocking only when its rank-128 updates are
-  // large enough to take the split tensor-core path
+  // the 128-wide blocking only for large inverses (n^2 128 >= 2^29 multiply-
+  // adds, complex counted 4x: n >= 2048 real, n >= 1024 complex); below that
+  // its extra launches and split passes cost more than the tensor cores
+  // save (measured on batches of blocks with n <= 1024), and the native
+  // elimination runs even when mixed precision is asked for
   const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8 &&
                      (traits<T>::cpx ? 4.0 : 1.0) * (double)n * (double)n * GJ_OUTER_NB >=
-                         SPLIT_MIN_MNK;
+                         8.0 * SPLIT_MIN_MNK;
   const int NBO = mixed ? GJ_OUTER_NB : GJ_NB;
   int* piv = ar.take<int>(n > 0 ? n : 1);
   real_t<T>* part_val = ar.take<real_t<T>>(sms);
