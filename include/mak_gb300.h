@@ -143,6 +143,42 @@ int mak_qr_full_c(int64_t m, int64_t n, void* A, int64_t lda, void* Q, int64_t l
                   void* R, int64_t ldr, const mak_qr_opts* opts, void* work,
                   size_t work_bytes, mak_info* info, mak_stream_t stream);
 
+/* -------------------------------------------------------------------- LQ ---
+ * lq_compact!(A, (L, Q), LQViaTransposedQR(GB300_HouseholderQR(; positive)))
+ * Replaces the reference's lq_compact! / lq_full! (src/implementations/lq.jl)
+ * through its transposed-QR algorithm (LQViaTransposedQR,
+ * src/interface/decompositions.jl:340-353): A = L Q is computed as the
+ * conjugate transpose of the QR of A^H.  A (m x n) is read, not destroyed.
+ * lq_compact: L m x min(m,n) (or NULL: not wanted), Q min(m,n) x n;
+ * lq_full: L m x n (or NULL), Q n x n.  positive = 1 gives diag(L) real >= 0.
+ */
+int mak_lq_workspace(int dtype, int64_t m, int64_t n, int full, const mak_qr_opts* opts,
+                     size_t* bytes);
+int mak_lq_compact_d(int64_t m, int64_t n, const double* A, int64_t lda, double* L, int64_t ldl,
+                     double* Q, int64_t ldq, const mak_qr_opts* opts, void* work,
+                     size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_compact_z(int64_t m, int64_t n, const void* A, int64_t lda, void* L, int64_t ldl,
+                     void* Q, int64_t ldq, const mak_qr_opts* opts, void* work,
+                     size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_compact_s(int64_t m, int64_t n, const float* A, int64_t lda, float* L, int64_t ldl,
+                     float* Q, int64_t ldq, const mak_qr_opts* opts, void* work,
+                     size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_compact_c(int64_t m, int64_t n, const void* A, int64_t lda, void* L, int64_t ldl,
+                     void* Q, int64_t ldq, const mak_qr_opts* opts, void* work,
+                     size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_full_d(int64_t m, int64_t n, const double* A, int64_t lda, double* L, int64_t ldl,
+                  double* Q, int64_t ldq, const mak_qr_opts* opts, void* work, size_t work_bytes,
+                  mak_info* info, mak_stream_t stream);
+int mak_lq_full_z(int64_t m, int64_t n, const void* A, int64_t lda, void* L, int64_t ldl,
+                  void* Q, int64_t ldq, const mak_qr_opts* opts, void* work, size_t work_bytes,
+                  mak_info* info, mak_stream_t stream);
+int mak_lq_full_s(int64_t m, int64_t n, const float* A, int64_t lda, float* L, int64_t ldl,
+                  float* Q, int64_t ldq, const mak_qr_opts* opts, void* work, size_t work_bytes,
+                  mak_info* info, mak_stream_t stream);
+int mak_lq_full_c(int64_t m, int64_t n, const void* A, int64_t lda, void* L, int64_t ldl,
+                  void* Q, int64_t ldq, const mak_qr_opts* opts, void* work, size_t work_bytes,
+                  mak_info* info, mak_stream_t stream);
+
 /* qr_compact! in Float64 that allocates nothing at call time.  It has no
  * counterpart in the reference (whose CUDA path lets CUSOLVER allocate its
  * own workspace).  For callers that cannot allocate device memory or keep a
@@ -213,6 +249,29 @@ int mak_left_polar_newton_s(int64_t m, int64_t n, float* A, int64_t lda, float* 
 int mak_left_polar_newton_c(int64_t m, int64_t n, void* A, int64_t lda, void* W, int64_t ldw,
                             void* P, int64_t ldp, const mak_polar_opts* opts, void* work,
                             size_t work_bytes, mak_info* info, mak_stream_t stream);
+
+/* right_polar!(A, (P, Wh), GB300_PolarNewton(; maxiter, tol))
+ * Replaces the reference's right_polar!(::PolarNewton) and
+ * right_polar_newton! (src/implementations/polar.jl:113-125,168-206):
+ * A = P Wh (n >= m required), computed as the conjugate transpose of the
+ * left polar decomposition A^H = Wh^H P, the same Newton iteration
+ * transposed.  A (m x n) is read, not destroyed.  P: m x m Hermitian, or NULL
+ * (not wanted).  Wh: m x n with orthonormal rows.  info as for the left form.
+ */
+int mak_right_polar_workspace(int dtype, int64_t m, int64_t n, int want_p,
+                              const mak_polar_opts* opts, size_t* bytes);
+int mak_right_polar_newton_d(int64_t m, int64_t n, const double* A, int64_t lda, double* P,
+                             int64_t ldp, double* Wh, int64_t ldwh, const mak_polar_opts* opts,
+                             void* work, size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_right_polar_newton_z(int64_t m, int64_t n, const void* A, int64_t lda, void* P,
+                             int64_t ldp, void* Wh, int64_t ldwh, const mak_polar_opts* opts,
+                             void* work, size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_right_polar_newton_s(int64_t m, int64_t n, const float* A, int64_t lda, float* P,
+                             int64_t ldp, float* Wh, int64_t ldwh, const mak_polar_opts* opts,
+                             void* work, size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_right_polar_newton_c(int64_t m, int64_t n, const void* A, int64_t lda, void* P,
+                             int64_t ldp, void* Wh, int64_t ldwh, const mak_polar_opts* opts,
+                             void* work, size_t work_bytes, mak_info* info, mak_stream_t stream);
 
 /* -------------------------------------------------------------- batched ---
  * Many independent, uneven blocks in one stream-ordered call (the symmetry
@@ -307,6 +366,96 @@ int mak_left_polar_pullback_c(int64_t m, int64_t n, void* dA, int64_t ldda, cons
                               int64_t lddw, const void* dP, int64_t lddp,
                               const mak_pullback_opts* opts, void* work, size_t work_bytes,
                               mak_info* info, mak_stream_t stream);
+
+/* right_polar_pullback!(dA, A, (P, Wh), (dP, dWh))
+ * Replaces the reference's right_polar_pullback! (src/pullbacks/polar.jl:
+ * 37-59): computed as the conjugate transpose of the left pullback of A^H at
+ * (Wh^H, P) with cotangents (dWh^H, dP), which carries the same Sylvester
+ * solve on the device.  m <= n.  dA (m x n) is accumulated into; dP / dWh may
+ * be NULL (a zero tangent).  Synchronizes `stream` once per sign iteration.
+ */
+int mak_right_polar_pullback_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                       size_t* bytes);
+int mak_right_polar_pullback_d(int64_t m, int64_t n, double* dA, int64_t ldda, const double* P,
+                               int64_t ldp, const double* Wh, int64_t ldwh, const double* dP,
+                               int64_t lddp, const double* dWh, int64_t lddwh,
+                               const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                               mak_info* info, mak_stream_t stream);
+int mak_right_polar_pullback_z(int64_t m, int64_t n, void* dA, int64_t ldda, const void* P,
+                               int64_t ldp, const void* Wh, int64_t ldwh, const void* dP,
+                               int64_t lddp, const void* dWh, int64_t lddwh,
+                               const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                               mak_info* info, mak_stream_t stream);
+int mak_right_polar_pullback_s(int64_t m, int64_t n, float* dA, int64_t ldda, const float* P,
+                               int64_t ldp, const float* Wh, int64_t ldwh, const float* dP,
+                               int64_t lddp, const float* dWh, int64_t lddwh,
+                               const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                               mak_info* info, mak_stream_t stream);
+int mak_right_polar_pullback_c(int64_t m, int64_t n, void* dA, int64_t ldda, const void* P,
+                               int64_t ldp, const void* Wh, int64_t ldwh, const void* dP,
+                               int64_t lddp, const void* dWh, int64_t lddwh,
+                               const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                               mak_info* info, mak_stream_t stream);
+
+/* left_polar_pushforward!(dA, A, (W, P), (dW, dP))
+ * Replaces the reference's left_polar_pushforward!
+ * (src/pushforwards/polar.jl:1-12): the tangent of A = W P along dA,
+ *   dP0 = W^H dA, K = sylvester(P, P, dP0^H - dP0), dW = (I - W W^H) dA P^-1
+ *   + W K, dP = dP0 - K P,
+ * with the Sylvester solve on the device (the pullback's sign iteration).
+ * m >= n.  dW (m x n) and dP (n x n) are outputs (overwritten).
+ */
+int mak_left_polar_pushforward_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                         size_t* bytes);
+int mak_left_polar_pushforward_d(int64_t m, int64_t n, const double* dA, int64_t ldda,
+                                 const double* W, int64_t ldw, const double* P, int64_t ldp,
+                                 double* dW, int64_t lddw, double* dP, int64_t lddp,
+                                 const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                 mak_info* info, mak_stream_t stream);
+int mak_left_polar_pushforward_z(int64_t m, int64_t n, const void* dA, int64_t ldda,
+                                 const void* W, int64_t ldw, const void* P, int64_t ldp,
+                                 void* dW, int64_t lddw, void* dP, int64_t lddp,
+                                 const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                 mak_info* info, mak_stream_t stream);
+int mak_left_polar_pushforward_s(int64_t m, int64_t n, const float* dA, int64_t ldda,
+                                 const float* W, int64_t ldw, const float* P, int64_t ldp,
+                                 float* dW, int64_t lddw, float* dP, int64_t lddp,
+                                 const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                 mak_info* info, mak_stream_t stream);
+int mak_left_polar_pushforward_c(int64_t m, int64_t n, const void* dA, int64_t ldda,
+                                 const void* W, int64_t ldw, const void* P, int64_t ldp,
+                                 void* dW, int64_t lddw, void* dP, int64_t lddp,
+                                 const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                 mak_info* info, mak_stream_t stream);
+
+/* right_polar_pushforward!(dA, A, (P, Wh), (dP, dWh))
+ * Replaces the reference's right_polar_pushforward!
+ * (src/pushforwards/polar.jl:14-26): the tangent of A = P Wh along dA,
+ * computed as the conjugate transpose of the left pushforward of A^H at
+ * (Wh^H, P) along dA^H.  m <= n.  dP (m x m) and dWh (m x n) are outputs.
+ */
+int mak_right_polar_pushforward_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                          size_t* bytes);
+int mak_right_polar_pushforward_d(int64_t m, int64_t n, const double* dA, int64_t ldda,
+                                  const double* P, int64_t ldp, const double* Wh, int64_t ldwh,
+                                  double* dP, int64_t lddp, double* dWh, int64_t lddwh,
+                                  const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                  mak_info* info, mak_stream_t stream);
+int mak_right_polar_pushforward_z(int64_t m, int64_t n, const void* dA, int64_t ldda,
+                                  const void* P, int64_t ldp, const void* Wh, int64_t ldwh,
+                                  void* dP, int64_t lddp, void* dWh, int64_t lddwh,
+                                  const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                  mak_info* info, mak_stream_t stream);
+int mak_right_polar_pushforward_s(int64_t m, int64_t n, const float* dA, int64_t ldda,
+                                  const float* P, int64_t ldp, const float* Wh, int64_t ldwh,
+                                  float* dP, int64_t lddp, float* dWh, int64_t lddwh,
+                                  const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                  mak_info* info, mak_stream_t stream);
+int mak_right_polar_pushforward_c(int64_t m, int64_t n, const void* dA, int64_t ldda,
+                                  const void* P, int64_t ldp, const void* Wh, int64_t ldwh,
+                                  void* dP, int64_t lddp, void* dWh, int64_t lddwh,
+                                  const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                  mak_info* info, mak_stream_t stream);
 
 #ifdef __cplusplus
 }

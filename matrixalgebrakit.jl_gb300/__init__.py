@@ -19,10 +19,11 @@ The directory name carries a dot, so load it with::
 
 from . import _lib
 from .algorithms import (ArgumentError, DimensionMismatch, GB300_HouseholderQR,
-                         GB300_PolarNewton, LeftOrthViaPolar, LeftOrthViaQR, default_algorithm,
-                         is_positive, select_algorithm)
+                         GB300_PolarNewton, LeftOrthViaPolar, LeftOrthViaQR, LQViaTransposedQR,
+                         default_algorithm, is_positive, select_algorithm)
 from .blas import gemm
-from .polar import SingularException, left_polar, left_polar_
+from .lq import lq_compact, lq_compact_, lq_full, lq_full_, lq_null, lq_null_
+from .polar import SingularException, left_polar, left_polar_, right_polar, right_polar_
 from .qr import (initialize_output, qr_compact, qr_compact_, qr_full, qr_full_, qr_null,
                  qr_null_)
 
@@ -31,6 +32,8 @@ __all__ = [
     "GB300_PolarNewton", "LeftOrthViaQR", "LeftOrthViaPolar", "default_algorithm",
     "select_algorithm", "is_positive", "qr_compact", "qr_compact_", "qr_full", "qr_full_",
     "qr_null", "qr_null_", "left_polar", "left_polar_", "initialize_output", "library", "gemm",
+    "LQViaTransposedQR", "lq_compact", "lq_compact_", "lq_full", "lq_full_", "lq_null",
+    "lq_null_", "right_polar", "right_polar_",
 ]
 
 
@@ -38,9 +41,11 @@ def library():
     """The loaded ctypes handle of libmak_gb300.so (raises if unavailable)."""
     return _lib.load()
 
-from .pullbacks import left_polar_pullback_, qr_pullback_  # noqa: E402
+from .pullbacks import left_polar_pullback_, qr_pullback_, right_polar_pullback_  # noqa: E402
+from .pushforwards import left_polar_pushforward_, right_polar_pushforward_  # noqa: E402
 
-__all__ += ["qr_pullback_", "left_polar_pullback_"]
+__all__ += ["qr_pullback_", "left_polar_pullback_", "right_polar_pullback_",
+            "left_polar_pushforward_", "right_polar_pushforward_"]
 
 from .batched import batched_left_polar, batched_qr_compact  # noqa: E402
 

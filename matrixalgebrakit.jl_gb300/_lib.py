@@ -90,6 +90,29 @@ _POLAR_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, C.POINTER(mak_polar_opt
 for _s in "dzsc":
     SIGNATURES[f"mak_left_polar_newton_{_s}"] = (C.c_int, _POLAR_ARGS)
 
+# LQ via the transposed QR and the right polar decomposition (transposed duals)
+SIGNATURES["mak_lq_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int, C.POINTER(mak_qr_opts),
+                                            C.POINTER(_sz)])
+SIGNATURES["mak_right_polar_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
+                                                     C.POINTER(mak_polar_opts), C.POINTER(_sz)])
+for _s in "dzsc":
+    for _kind in ("compact", "full"):
+        SIGNATURES[f"mak_lq_{_kind}_{_s}"] = (C.c_int, _QR_ARGS)
+    SIGNATURES[f"mak_right_polar_newton_{_s}"] = (C.c_int, _POLAR_ARGS)
+# right polar pullback and left polar pushforward
+_PB_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64,
+            C.POINTER(mak_pullback_opts), _p, _sz, _p, _p]
+SIGNATURES["mak_right_polar_pullback_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
+                                                              C.POINTER(_sz)])
+SIGNATURES["mak_left_polar_pushforward_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
+                                                                C.POINTER(_sz)])
+for _s in "dzsc":
+    SIGNATURES[f"mak_right_polar_pullback_{_s}"] = (C.c_int, _PB_ARGS)
+    SIGNATURES[f"mak_left_polar_pushforward_{_s}"] = (C.c_int, _PB_ARGS)
+    SIGNATURES[f"mak_right_polar_pushforward_{_s}"] = (C.c_int, _PB_ARGS)
+SIGNATURES["mak_right_polar_pushforward_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
+                                                                 C.POINTER(_sz)])
+
 _lib = None
 _load_error = None
 

@@ -68,6 +68,21 @@ class GB300_PolarNewton:
 
 
 @dataclass(frozen=True)
+class LQViaTransposedQR:
+    """``LQViaTransposedQR(qr_alg)`` (src/interface/decompositions.jl:340-353):
+    the LQ of A as the conjugate transpose of the QR of A^H.  A bare
+    ``GB300_HouseholderQR`` given to an ``lq_*`` function is wrapped in it, as
+    the reference routes its GPU Householder drivers through ``lq_via_qr!``
+    (src/implementations/lq.jl:130-131)."""
+
+    alg: GB300_HouseholderQR = field(default_factory=GB300_HouseholderQR)
+
+    @property
+    def positive(self) -> bool:
+        return self.alg.positive
+
+
+@dataclass(frozen=True)
 class LeftOrthViaQR:
     """``left_orth`` through a QR algorithm (src/interface/decompositions.jl:556-577)."""
 
@@ -84,7 +99,8 @@ class LeftOrthViaPolar:
 ALGORITHMS = {c.__name__: c for c in (GB300_HouseholderQR, GB300_PolarNewton)}
 
 _QR_FUNCS = ("qr_compact", "qr_compact_", "qr_full", "qr_full_", "qr_null", "qr_null_")
-_POLAR_FUNCS = ("left_polar", "left_polar_")
+_LQ_FUNCS = ("lq_compact", "lq_compact_", "lq_full", "lq_full_", "lq_null", "lq_null_")
+_POLAR_FUNCS = ("left_polar", "left_polar_", "right_polar", "right_polar_")
 
 
 def _fname(f) -> str:
@@ -98,6 +114,8 @@ def default_algorithm(f, A=None, **kwargs):
     name = _fname(f)
     if name in _QR_FUNCS:
         return GB300_HouseholderQR(**kwargs)
+    if name in _LQ_FUNCS:
+        return LQViaTransposedQR(GB300_HouseholderQR(**kwargs))
     if name in _POLAR_FUNCS:
         return GB300_PolarNewton(**kwargs)
     if name in ("left_orth", "left_orth_"):
@@ -112,20 +130,28 @@ def select_algorithm(f, A=None, alg=None, **kwargs):
     if isinstance(alg, str):
         if alg not in ALGORITHMS:
             raise ArgumentError(f"Unknown alg {alg}")
-        return ALGORITHMS[alg](**kwargs)
+        return _lq_wrap(f, ALGORITHMS[alg](**kwargs))
     if isinstance(alg, type):
-        return alg(**kwargs)
+        return _lq_wrap(f, alg(**kwargs))
     if isinstance(alg, dict):
         if kwargs:
             raise ArgumentError("Additional keyword arguments are not allowed when algorithm "
                                 "parameters are specified.")
         return default_algorithm(f, A, **alg)
-    if isinstance(alg, (GB300_HouseholderQR, GB300_PolarNewton, LeftOrthViaQR, LeftOrthViaPolar)):
+    if isinstance(alg, (GB300_HouseholderQR, GB300_PolarNewton, LeftOrthViaQR, LeftOrthViaPolar,
+                        LQViaTransposedQR)):
         if kwargs:
             raise ArgumentError("Additional keyword arguments are not allowed when algorithm "
                                 "parameters are specified.")
-        return alg
+        return _lq_wrap(f, alg)
     raise ArgumentError(f"Unknown alg {alg}")
+
+
+def _lq_wrap(f, alg):
+    """A QR algorithm given to an lq_* function means the transposed QR."""
+    if _fname(f) in _LQ_FUNCS and isinstance(alg, GB300_HouseholderQR):
+        return LQViaTransposedQR(alg)
+    return alg
 
 
 def is_positive(alg) -> bool:

@@ -317,23 +317,29 @@ int qr_pullback_run(cudaStream_t st, int64_t m, int64_t n, int full, T* dA, int6
 }
 
 // ----------------------------------------------------------- polar pullback --
+// Scratch of the device Sylvester solve (and of the products around it).
 template <class T>
-int polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldda, const T* W,
-                       int64_t ldw, const T* P, int64_t ldp, const T* dW, int64_t lddw,
-                       const T* dP, int64_t lddp, int maxiter, int precision, Arena& ar,
-                       mak_info* info) {
+struct SylScratch {
+  real_t<T>* scal;
+  T *Mm, *Ak, *Ck, *Ai, *Tm, *Y, *Pinv;
+  int* iperm;
+  char* tail;
+  size_t tail_bytes;
+};
+template <class T>
+static SylScratch<T> syl_take(Arena& ar, cudaStream_t st, int64_t m, int64_t n, int precision) {
   using Rr = real_t<T>;
   const size_t nn = (size_t)n * n;
-  Rr* scal = ar.take<Rr>(RED_CTAS + 16);
-  T* dPh = ar.take<T>(nn + 1);
-  T* Mm = ar.take<T>(nn + 1);
-  T* Ak = ar.take<T>(nn + 1);
-  T* Ck = ar.take<T>(nn + 1);
-  T* Ai = ar.take<T>(nn + 1);
-  T* Pinv = ar.take<T>(nn + 1);
-  T* Tm = ar.take<T>(nn + 1);
-  T* Y = ar.take<T>((size_t)m * n + 1);
-  int* iperm = ar.take<int>(n + 1);
+  SylScratch<T> s;
+  s.scal = ar.take<Rr>(RED_CTAS + 16);
+  s.Mm = ar.take<T>(nn + 1);
+  s.Ak = ar.take<T>(nn + 1);
+  s.Ck = ar.take<T>(nn + 1);
+  s.Ai = ar.take<T>(nn + 1);
+  s.Pinv = ar.take<T>(nn + 1);
+  s.Tm = ar.take<T>(nn + 1);
+  s.Y = ar.take<T>((size_t)m * n + 1);
+  s.iperm = ar.take<int>(n + 1);
   size_t gj_ws = 0, oz_ws = 0;
   {
     Arena meas(nullptr, 0);
@@ -347,29 +353,98 @@ int polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldd
       if (m2.off + 256 > oz_ws) oz_ws = m2.off + 256;
     }
   }
-  const size_t tail_bytes = gj_ws > oz_ws ? gj_ws : oz_ws;
-  char* tail = ar.take<char>(tail_bytes);
+  s.tail_bytes = gj_ws > oz_ws ? gj_ws : oz_ws;
+  s.tail = ar.take<char>(s.tail_bytes);
+  return s;
+}
+
+// Solves P X + X P = M - M^H for X (n x n, ld n) with P Hermitian positive
+// definite, by the sign-function Newton iteration on [[P, -C], [0, -P]]
+// carried on its two blocks (A_k, C_k): A_{k+1} = (A_k + A_k^-1)/2,
+// C_{k+1} = (C_k + A_k^-1 C_k A_k^-1)/2 from A_0 = P, C_0 = -(M - M^H);
+// the solution is X = -C_inf / 2.  M is read from s.Mm (ld n); P^-1 (the
+// first iterate's inverse) is left in s.Pinv; X goes to s.Tm.  The host
+// synchronizes once per iteration for the stopping test.
+template <class T>
+static int syl_solve(cudaStream_t st, int64_t n, const T* P, int64_t ldp, int maxiter,
+                     int precision, SylScratch<T>& s, mak_info* info, int* iters) {
+  using Rr = real_t<T>;
+  const size_t nn = (size_t)n * n;
+  int* status = &info->status;
+  Rr* red = s.scal;
+  Rr* nrm2 = s.scal + RED_CTAS;  // [0] ||A||^2, [1] ||Ai||^2, [2] ||dA||^2
+  auto G = [&](int64_t M_, int64_t N_, int64_t K_, T alpha, Operand<T> a, Operand<T> b, T beta,
+               T* C_, int64_t ldc) -> int {
+    Arena oz(s.tail, s.tail_bytes);
+    return gemm_prec<T>(st, precision, M_, N_, K_, alpha, a, b, beta, C_, ldc, oz, status);
+  };
+  auto inverse = [&](const T* X, T* out) -> int {
+    MAK_TRY(copy_mat<T>(st, n, n, X, n, s.Tm, n));
+    {
+      Arena gj(s.tail, s.tail_bytes);
+      MAK_TRY(gje_inverse<T>(st, n, s.Tm, n, s.iperm, precision, gj, info));
+    }
+    note_launch();
+    gather_cols_kernel<T><<<dim3((unsigned)ceil_div(n, 128), (unsigned)n), 128, 0, st>>>(
+        (int)n, s.Tm, n, s.iperm, out, n);
+    return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+  };
+  const unsigned g1 = (unsigned)ceil_div((int64_t)nn, 256);
+  // C_0 = -(M - M^H), A_0 = P
+  {
+    dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+    note_launch();
+    antiherm_kernel<T><<<g, 256, 0, st>>>((int)n, s.Mm, n, Rr(-1), s.Ck, n);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
+  MAK_TRY(copy_mat<T>(st, n, n, P, ldp, s.Ak, n));
+  const Rr tol = (sizeof(Rr) == 8 ? Rr(1e-13) : Rr(1e-6)) * sqrt((Rr)n);
+  int it = 0;
+  for (it = 1; it <= maxiter; it++) {
+    MAK_TRY(inverse(s.Ak, s.Ai));
+    if (it == 1) MAK_TRY(copy_mat<T>(st, n, n, s.Ai, n, s.Pinv, n));
+    MAK_TRY(reduce_mat<T>(st, n, n, s.Ak, n, 0, red, nrm2));
+    MAK_TRY(reduce_mat<T>(st, n, n, s.Ai, n, 0, red, nrm2 + 1));
+    // Tm = Ai C Ai
+    MAK_TRY(G(n, n, n, one_<T>(), opnd<T>(s.Ai, n), opnd<T>(s.Ck, n), zero_<T>(), s.Y, n));
+    MAK_TRY(G(n, n, n, one_<T>(), opnd<T>(s.Y, n), opnd<T>(s.Ai, n), zero_<T>(), s.Tm, n));
+    const unsigned gr = g1 < RED_CTAS ? g1 : RED_CTAS;
+    note_launch();
+    sign_update_kernel<T><<<gr, 256, 0, st>>>((int64_t)nn, s.Ak, s.Ai, s.Ck, s.Tm, nrm2, red);
+    MAK_CUDA_TRY(cudaGetLastError());
+    note_launch();
+    reduce_final_kernel<Rr><<<1, 256, 0, st>>>((int)gr, red, 0, nrm2 + 2);
+    MAK_CUDA_TRY(cudaGetLastError());
+    MAK_TRY(herm_project<T>(st, n, s.Ak, n));
+    Rr dnorm2 = 0;
+    MAK_CUDA_TRY(cudaMemcpyAsync(&dnorm2, nrm2 + 2, sizeof(Rr), cudaMemcpyDeviceToHost, st));
+    MAK_CUDA_TRY(cudaStreamSynchronize(st));
+    if (!(sqrt(dnorm2) > tol)) break;
+  }
+  if (it > maxiter) it = maxiter;
+  *iters = it;
+  // X = -C_inf / 2
+  note_launch();
+  scale_copy_kernel<T><<<g1, 256, 0, st>>>((int64_t)nn, s.Ck, Rr(-0.5), s.Tm);
+  return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+}
+
+template <class T>
+int polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldda, const T* W,
+                       int64_t ldw, const T* P, int64_t ldp, const T* dW, int64_t lddw,
+                       const T* dP, int64_t lddp, int maxiter, int precision, Arena& ar,
+                       mak_info* info) {
+  const size_t nn = (size_t)n * n;
+  T* dPh = ar.take<T>(nn + 1);
+  SylScratch<T> s = syl_take<T>(ar, st, m, n, precision);
   if (ar.base == nullptr) return 0;
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
   if (n == 0) return 0;
   int* status = &info->status;
-  Rr* red = scal;
-  Rr* nrm2 = scal + RED_CTAS;  // [0] ||A||^2, [1] ||Ai||^2, [2] ||dA||^2
   auto G = [&](int64_t M_, int64_t N_, int64_t K_, T alpha, Operand<T> a, Operand<T> b, T beta,
                T* C_, int64_t ldc) -> int {
-    Arena oz(tail, tail_bytes);
+    Arena oz(s.tail, s.tail_bytes);
     return gemm_prec<T>(st, precision, M_, N_, K_, alpha, a, b, beta, C_, ldc, oz, status);
-  };
-  auto inverse = [&](const T* X, T* out) -> int {
-    MAK_TRY(copy_mat<T>(st, n, n, X, n, Tm, n));
-    {
-      Arena gj(tail, tail_bytes);
-      MAK_TRY(gje_inverse<T>(st, n, Tm, n, iperm, precision, gj, info));
-    }
-    note_launch();
-    gather_cols_kernel<T><<<dim3((unsigned)ceil_div(n, 128), (unsigned)n), 128, 0, st>>>(
-        (int)n, Tm, n, iperm, out, n);
-    return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
   };
   const unsigned g1 = (unsigned)ceil_div((int64_t)nn, 256);
 
@@ -379,67 +454,71 @@ int polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldd
     MAK_TRY(herm_project<T>(st, n, dPh, n));
   }
   if (dW)
-    MAK_TRY(G(n, n, m, one_<T>(), opnd<T>(W, ldw, OP_C), opnd<T>(dW, lddw), zero_<T>(), Mm, n));
+    MAK_TRY(G(n, n, m, one_<T>(), opnd<T>(W, ldw, OP_C), opnd<T>(dW, lddw), zero_<T>(), s.Mm, n));
   else
-    MAK_CUDA_TRY(cudaMemsetAsync(Mm, 0, nn * sizeof(T), st));
+    MAK_CUDA_TRY(cudaMemsetAsync(s.Mm, 0, nn * sizeof(T), st));
   if (dP)
-    MAK_TRY(G(n, n, n, -one_<T>(), opnd<T>(dPh, n), opnd<T>(P, ldp), one_<T>(), Mm, n));
-  // C_0 = -(M - M^H), A_0 = P
-  {
-    dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
-    note_launch();
-    antiherm_kernel<T><<<g, 256, 0, st>>>((int)n, Mm, n, Rr(-1), Ck, n);
-    MAK_CUDA_TRY(cudaGetLastError());
-  }
-  MAK_TRY(copy_mat<T>(st, n, n, P, ldp, Ak, n));
-
-  // sign-function Newton iteration
-  const Rr tol = (sizeof(Rr) == 8 ? Rr(1e-13) : Rr(1e-6)) * sqrt((Rr)n);
+    MAK_TRY(G(n, n, n, -one_<T>(), opnd<T>(dPh, n), opnd<T>(P, ldp), one_<T>(), s.Mm, n));
+  // C = sylvester(P, P, M^H - M):  P C + C P = M - M^H
   int it = 0;
-  for (it = 1; it <= maxiter; it++) {
-    MAK_TRY(inverse(Ak, Ai));
-    if (it == 1) MAK_TRY(copy_mat<T>(st, n, n, Ai, n, Pinv, n));
-    MAK_TRY(reduce_mat<T>(st, n, n, Ak, n, 0, red, nrm2));
-    MAK_TRY(reduce_mat<T>(st, n, n, Ai, n, 0, red, nrm2 + 1));
-    // Tm = Ai C Ai
-    MAK_TRY(G(n, n, n, one_<T>(), opnd<T>(Ai, n), opnd<T>(Ck, n), zero_<T>(), Y, n));
-    MAK_TRY(G(n, n, n, one_<T>(), opnd<T>(Y, n), opnd<T>(Ai, n), zero_<T>(), Tm, n));
-    const unsigned gr = g1 < RED_CTAS ? g1 : RED_CTAS;
-    note_launch();
-    sign_update_kernel<T><<<gr, 256, 0, st>>>((int64_t)nn, Ak, Ai, Ck, Tm, nrm2, red);
-    MAK_CUDA_TRY(cudaGetLastError());
-    note_launch();
-    reduce_final_kernel<Rr><<<1, 256, 0, st>>>((int)gr, red, 0, nrm2 + 2);
-    MAK_CUDA_TRY(cudaGetLastError());
-    MAK_TRY(herm_project<T>(st, n, Ak, n));
-    Rr dnorm2 = 0;
-    MAK_CUDA_TRY(cudaMemcpyAsync(&dnorm2, nrm2 + 2, sizeof(Rr), cudaMemcpyDeviceToHost, st));
-    MAK_CUDA_TRY(cudaStreamSynchronize(st));
-    if (!(sqrt(dnorm2) > tol)) break;
-  }
-  if (it > maxiter) it = maxiter;
-  // C = -C_inf/2 (+ dP);  dA += W C
-  note_launch();
-  scale_copy_kernel<T><<<g1, 256, 0, st>>>((int64_t)nn, Ck, Rr(-0.5), Tm);
-  MAK_CUDA_TRY(cudaGetLastError());
+  MAK_TRY(syl_solve<T>(st, n, P, ldp, maxiter, precision, s, info, &it));
   if (dP) {
     note_launch();
-    add_kernel<T><<<g1, 256, 0, st>>>((int64_t)nn, dPh, Tm);
+    add_kernel<T><<<g1, 256, 0, st>>>((int64_t)nn, dPh, s.Tm);
     MAK_CUDA_TRY(cudaGetLastError());
   }
-  MAK_TRY(G(m, n, n, one_<T>(), opnd<T>(W, ldw), opnd<T>(Tm, n), one_<T>(), dA, ldda));
+  // dA += W C
+  MAK_TRY(G(m, n, n, one_<T>(), opnd<T>(W, ldw), opnd<T>(s.Tm, n), one_<T>(), dA, ldda));
   // dA += (I - W W^H) dW P^{-1}
   if (dW) {
-    MAK_TRY(G(m, n, n, one_<T>(), opnd<T>(dW, lddw), opnd<T>(Pinv, n), zero_<T>(), Y, m));
-    MAK_TRY(G(n, n, m, one_<T>(), opnd<T>(W, ldw, OP_C), opnd<T>(Y, m), zero_<T>(), Mm, n));
-    MAK_TRY(G(m, n, n, -one_<T>(), opnd<T>(W, ldw), opnd<T>(Mm, n), one_<T>(), Y, m));
+    MAK_TRY(G(m, n, n, one_<T>(), opnd<T>(dW, lddw), opnd<T>(s.Pinv, n), zero_<T>(), s.Y, m));
+    MAK_TRY(G(n, n, m, one_<T>(), opnd<T>(W, ldw, OP_C), opnd<T>(s.Y, m), zero_<T>(), s.Mm, n));
+    MAK_TRY(G(m, n, n, -one_<T>(), opnd<T>(W, ldw), opnd<T>(s.Mm, n), one_<T>(), s.Y, m));
     {
       dim3 g((unsigned)ceil_div(m, 256), (unsigned)(n < 65535 ? n : 65535));
       note_launch();
-      add_strided_kernel<T><<<g, 256, 0, st>>>(m, n, Y, m, dA, ldda);
+      add_strided_kernel<T><<<g, 256, 0, st>>>(m, n, s.Y, m, dA, ldda);
       MAK_CUDA_TRY(cudaGetLastError());
     }
   }
+  note_launch();
+  info_pullback_kernel<T><<<1, 1, 0, st>>>(info, (int)n, it, nullptr, nullptr);
+  MAK_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// left_polar_pushforward!: the tangent (dW, dP) of the left polar
+// decomposition A = W P along dA (reference src/pushforwards/polar.jl:1-12):
+//   dP0 = W^H dA,  K = sylvester(P, P, dP0^H - dP0)  (P K + K P = dP0 - dP0^H),
+//   dW = (I - W W^H) dA P^-1 + W K,  dP = dP0 - K P.
+// dW (m x n) and dP (n x n) are outputs (overwritten).
+template <class T>
+int polar_pushforward_run(cudaStream_t st, int64_t m, int64_t n, const T* dA, int64_t ldda,
+                          const T* W, int64_t ldw, const T* P, int64_t ldp, T* dW, int64_t lddw,
+                          T* dP, int64_t lddp, int maxiter, int precision, Arena& ar,
+                          mak_info* info) {
+  SylScratch<T> s = syl_take<T>(ar, st, m, n, precision);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  if (n == 0) return 0;
+  int* status = &info->status;
+  auto G = [&](int64_t M_, int64_t N_, int64_t K_, T alpha, Operand<T> a, Operand<T> b, T beta,
+               T* C_, int64_t ldc) -> int {
+    Arena oz(s.tail, s.tail_bytes);
+    return gemm_prec<T>(st, precision, M_, N_, K_, alpha, a, b, beta, C_, ldc, oz, status);
+  };
+  // dP = W^H dA (kept for the end), M = the same
+  MAK_TRY(G(n, n, m, one_<T>(), opnd<T>(W, ldw, OP_C), opnd<T>(dA, ldda), zero_<T>(), dP, lddp));
+  MAK_TRY(copy_mat<T>(st, n, n, dP, lddp, s.Mm, n));
+  int it = 0;
+  MAK_TRY(syl_solve<T>(st, n, P, ldp, maxiter, precision, s, info, &it));  // K in s.Tm
+  // dW = dA P^-1;  dW -= W (W^H dW);  dW += W K
+  MAK_TRY(G(m, n, n, one_<T>(), opnd<T>(dA, ldda), opnd<T>(s.Pinv, n), zero_<T>(), dW, lddw));
+  MAK_TRY(G(n, n, m, one_<T>(), opnd<T>(W, ldw, OP_C), opnd<T>(dW, lddw), zero_<T>(), s.Mm, n));
+  MAK_TRY(G(m, n, n, -one_<T>(), opnd<T>(W, ldw), opnd<T>(s.Mm, n), one_<T>(), dW, lddw));
+  MAK_TRY(G(m, n, n, one_<T>(), opnd<T>(W, ldw), opnd<T>(s.Tm, n), one_<T>(), dW, lddw));
+  // dP -= K P
+  MAK_TRY(G(n, n, n, -one_<T>(), opnd<T>(s.Tm, n), opnd<T>(P, ldp), one_<T>(), dP, lddp));
   note_launch();
   info_pullback_kernel<T><<<1, 1, 0, st>>>(info, (int)n, it, nullptr, nullptr);
   MAK_CUDA_TRY(cudaGetLastError());
@@ -519,6 +598,199 @@ static int polar_pullback_entry(int64_t m, int64_t n, void* dAv, int64_t ldda, c
 }
 
 template <class T>
+static int polar_pushforward_entry(int64_t m, int64_t n, const void* dAv, int64_t ldda,
+                                   const void* Wv, int64_t ldw, const void* Pv, int64_t ldp,
+                                   void* dWv, int64_t lddw, void* dPv, int64_t lddp,
+                                   const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                   mak_info* info, mak_stream_t stream) {
+  if (m < 0) return -1;
+  if (n < 0 || n > m) return -2;
+  if (dAv == nullptr && m * n > 0) return -3;
+  if (ldda < (m > 1 ? m : 1)) return -4;
+  if (Wv == nullptr && m * n > 0) return -5;
+  if (ldw < (m > 1 ? m : 1)) return -6;
+  if (Pv == nullptr && n > 0) return -7;
+  if (ldp < (n > 1 ? n : 1)) return -8;
+  if (dWv == nullptr && m * n > 0) return -9;
+  if (lddw < (m > 1 ? m : 1)) return -10;
+  if (dPv == nullptr && n > 0) return -11;
+  if (lddp < (n > 1 ? n : 1)) return -12;
+  mak_pullback_opts o{-1.0, -1.0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -13;
+  if (info == nullptr) return -16;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    polar_pushforward_run<T>(st, m, n, nullptr, ldda, nullptr, ldw, nullptr, ldp, nullptr, lddw,
+                             nullptr, lddp, SIGN_MAXITER, o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -15;
+  }
+  MAK_TRY(info_reset(st, info));
+  Arena ar(work, work_bytes);
+  return polar_pushforward_run<T>(st, m, n, (const T*)dAv, ldda, (const T*)Wv, ldw,
+                                  (const T*)Pv, ldp, (T*)dWv, lddw, (T*)dPv, lddp, SIGN_MAXITER,
+                                  o.precision, ar, info);
+}
+
+// right_polar_pullback! (reference src/pullbacks/polar.jl:37-59) as the left
+// pullback of A^H: right_polar(A) = (P, Wh) is left_polar(A^H) = (Wh^H, P),
+// and the cotangent pairing is preserved by the conjugate transpose, so
+// dA += (left_polar_pullback of A^H at (Wh^H, P) with (dWh^H, dP))^H.
+template <class T>
+static int right_polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldda,
+                                    const T* P, int64_t ldp, const T* Wh, int64_t ldwh,
+                                    const T* dP, int64_t lddp, const T* dWh, int64_t lddwh,
+                                    int precision, Arena& ar, mak_info* info) {
+  T* Wt = ar.take<T>((size_t)n * m + 1);
+  T* dWt = ar.take<T>((size_t)n * m + 1);
+  T* dB = ar.take<T>((size_t)n * m + 1);
+  size_t inner = 0;
+  {
+    Arena meas(nullptr, 0);
+    polar_pullback_run<T>(st, n, m, nullptr, n, nullptr, n, nullptr, m, nullptr, n, nullptr, m,
+                          SIGN_MAXITER, precision, meas, nullptr);
+    inner = meas.off + 256;
+  }
+  char* sub = ar.take<char>(inner);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  if (m == 0 || n == 0) return 0;
+  MAK_TRY(ctranspose<T>(st, m, n, Wh, ldwh, Wt, n));
+  if (dWh) MAK_TRY(ctranspose<T>(st, m, n, dWh, lddwh, dWt, n));
+  MAK_CUDA_TRY(cudaMemsetAsync(dB, 0, (size_t)n * m * sizeof(T), st));
+  Arena a2(sub, inner);
+  MAK_TRY(polar_pullback_run<T>(st, n, m, dB, n, Wt, n, P, ldp, dWh ? dWt : nullptr, n, dP, lddp,
+                                SIGN_MAXITER, precision, a2, info));
+  return ctranspose<T>(st, n, m, dB, n, dA, ldda, true);
+}
+
+template <class T>
+static int right_polar_pullback_entry(int64_t m, int64_t n, void* dAv, int64_t ldda,
+                                      const void* Pv, int64_t ldp, const void* Whv, int64_t ldwh,
+                                      const void* dPv, int64_t lddp, const void* dWhv,
+                                      int64_t lddwh, const mak_pullback_opts* opts, void* work,
+                                      size_t work_bytes, mak_info* info, mak_stream_t stream) {
+  if (m < 0) return -1;
+  if (n < m) return -2;
+  if (dAv == nullptr && m * n > 0) return -3;
+  if (ldda < (m > 1 ? m : 1)) return -4;
+  if (Pv == nullptr && m > 0) return -5;
+  if (ldp < (m > 1 ? m : 1)) return -6;
+  if (Whv == nullptr && m * n > 0) return -7;
+  if (ldwh < (m > 1 ? m : 1)) return -8;
+  if (dPv && lddp < (m > 1 ? m : 1)) return -10;
+  if (dWhv && lddwh < (m > 1 ? m : 1)) return -12;
+  mak_pullback_opts o{-1.0, -1.0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -13;
+  if (info == nullptr) return -16;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    right_polar_pullback_run<T>(st, m, n, nullptr, ldda, nullptr, ldp, nullptr, ldwh, nullptr,
+                                lddp, nullptr, lddwh, o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -15;
+  }
+  MAK_TRY(info_reset(st, info));
+  Arena ar(work, work_bytes);
+  return right_polar_pullback_run<T>(st, m, n, (T*)dAv, ldda, (const T*)Pv, ldp, (const T*)Whv,
+                                     ldwh, (const T*)dPv, lddp, (const T*)dWhv, lddwh,
+                                     o.precision, ar, info);
+}
+
+// right_polar_pushforward! (reference src/pushforwards/polar.jl:14-26) as the
+// left pushforward of A^H at (Wh^H, P) along dA^H: the returned tangents are
+// the conjugate transposes (dWh = dW'^H, dP = dP'^H).  m <= n.
+template <class T>
+static int right_polar_pushforward_run(cudaStream_t st, int64_t m, int64_t n, const T* dA,
+                                       int64_t ldda, const T* P, int64_t ldp, const T* Wh,
+                                       int64_t ldwh, T* dP, int64_t lddp, T* dWh, int64_t lddwh,
+                                       int precision, Arena& ar, mak_info* info) {
+  T* dAt = ar.take<T>((size_t)n * m + 1);
+  T* Wt = ar.take<T>((size_t)n * m + 1);
+  T* dWt = ar.take<T>((size_t)n * m + 1);
+  T* dPt = ar.take<T>((size_t)m * m + 1);
+  size_t inner = 0;
+  {
+    Arena meas(nullptr, 0);
+    polar_pushforward_run<T>(st, n, m, nullptr, n, nullptr, n, nullptr, m, nullptr, n, nullptr, m,
+                             SIGN_MAXITER, precision, meas, nullptr);
+    inner = meas.off + 256;
+  }
+  char* sub = ar.take<char>(inner);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  if (m == 0 || n == 0) return 0;
+  MAK_TRY(ctranspose<T>(st, m, n, dA, ldda, dAt, n));
+  MAK_TRY(ctranspose<T>(st, m, n, Wh, ldwh, Wt, n));
+  Arena a2(sub, inner);
+  MAK_TRY(polar_pushforward_run<T>(st, n, m, dAt, n, Wt, n, P, ldp, dWt, n, dPt, m, SIGN_MAXITER,
+                                   precision, a2, info));
+  MAK_TRY(ctranspose<T>(st, n, m, dWt, n, dWh, lddwh));
+  return ctranspose<T>(st, m, m, dPt, m, dP, lddp);
+}
+
+template <class T>
+static int right_polar_pushforward_entry(int64_t m, int64_t n, const void* dAv, int64_t ldda,
+                                         const void* Pv, int64_t ldp, const void* Whv,
+                                         int64_t ldwh, void* dPv, int64_t lddp, void* dWhv,
+                                         int64_t lddwh, const mak_pullback_opts* opts, void* work,
+                                         size_t work_bytes, mak_info* info, mak_stream_t stream) {
+  if (m < 0) return -1;
+  if (n < m) return -2;
+  if (dAv == nullptr && m * n > 0) return -3;
+  if (ldda < (m > 1 ? m : 1)) return -4;
+  if (Pv == nullptr && m > 0) return -5;
+  if (ldp < (m > 1 ? m : 1)) return -6;
+  if (Whv == nullptr && m * n > 0) return -7;
+  if (ldwh < (m > 1 ? m : 1)) return -8;
+  if (dPv == nullptr && m > 0) return -9;
+  if (lddp < (m > 1 ? m : 1)) return -10;
+  if (dWhv == nullptr && m * n > 0) return -11;
+  if (lddwh < (m > 1 ? m : 1)) return -12;
+  mak_pullback_opts o{-1.0, -1.0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -13;
+  if (info == nullptr) return -16;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    right_polar_pushforward_run<T>(st, m, n, nullptr, ldda, nullptr, ldp, nullptr, ldwh, nullptr,
+                                   lddp, nullptr, lddwh, o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -15;
+  }
+  MAK_TRY(info_reset(st, info));
+  Arena ar(work, work_bytes);
+  return right_polar_pushforward_run<T>(st, m, n, (const T*)dAv, ldda, (const T*)Pv, ldp,
+                                        (const T*)Whv, ldwh, (T*)dPv, lddp, (T*)dWhv, lddwh,
+                                        o.precision, ar, info);
+}
+
+template <class T>
+static size_t rpolar_pf_ws(int64_t m, int64_t n, int prec) {
+  Arena meas(nullptr, 0);
+  right_polar_pushforward_run<T>(0, m, n, nullptr, m, nullptr, m, nullptr, m, nullptr, m, nullptr,
+                                 m, prec, meas, nullptr);
+  return meas.off + 256;
+}
+
+template <class T>
+static size_t polar_pf_ws(int64_t m, int64_t n, int prec) {
+  Arena meas(nullptr, 0);
+  polar_pushforward_run<T>(0, m, n, nullptr, m, nullptr, m, nullptr, n, nullptr, m, nullptr, n,
+                           SIGN_MAXITER, prec, meas, nullptr);
+  return meas.off + 256;
+}
+template <class T>
+static size_t rpolar_pb_ws(int64_t m, int64_t n, int prec) {
+  Arena meas(nullptr, 0);
+  right_polar_pullback_run<T>(0, m, n, nullptr, m, nullptr, m, nullptr, m, nullptr, m, nullptr,
+                              m, prec, meas, nullptr);
+  return meas.off + 256;
+}
+
+template <class T>
 static size_t qr_pb_ws(int64_t m, int64_t n, int full, int prec) {
   Arena meas(nullptr, 0);
   qr_pullback_run<T>(0, m, n, full, nullptr, m, nullptr, m, nullptr, m, nullptr, m, nullptr, m,
@@ -594,5 +866,89 @@ MAK_POLPB(mak_left_polar_pullback_d, double, double)
 MAK_POLPB(mak_left_polar_pullback_z, zcomplex, void)
 MAK_POLPB(mak_left_polar_pullback_s, float, float)
 MAK_POLPB(mak_left_polar_pullback_c, ccomplex, void)
+
+int mak_left_polar_pushforward_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                         size_t* bytes) {
+  if (bytes == nullptr) return -5;
+  if (m < 0) return -2;
+  if (n < 0 || n > m) return -3;
+  switch (dtype) {
+    case MAK_F64: *bytes = polar_pf_ws<double>(m, n, precision); break;
+    case MAK_C64: *bytes = polar_pf_ws<zcomplex>(m, n, precision); break;
+    case MAK_F32: *bytes = polar_pf_ws<float>(m, n, precision); break;
+    case MAK_C32: *bytes = polar_pf_ws<ccomplex>(m, n, precision); break;
+    default: return -1;
+  }
+  return 0;
+}
+
+int mak_right_polar_pullback_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                       size_t* bytes) {
+  if (bytes == nullptr) return -5;
+  if (m < 0) return -2;
+  if (n < m) return -3;
+  switch (dtype) {
+    case MAK_F64: *bytes = rpolar_pb_ws<double>(m, n, precision); break;
+    case MAK_C64: *bytes = rpolar_pb_ws<zcomplex>(m, n, precision); break;
+    case MAK_F32: *bytes = rpolar_pb_ws<float>(m, n, precision); break;
+    case MAK_C32: *bytes = rpolar_pb_ws<ccomplex>(m, n, precision); break;
+    default: return -1;
+  }
+  return 0;
+}
+
+int mak_right_polar_pushforward_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                          size_t* bytes) {
+  if (bytes == nullptr) return -5;
+  if (m < 0) return -2;
+  if (n < m) return -3;
+  switch (dtype) {
+    case MAK_F64: *bytes = rpolar_pf_ws<double>(m, n, precision); break;
+    case MAK_C64: *bytes = rpolar_pf_ws<zcomplex>(m, n, precision); break;
+    case MAK_F32: *bytes = rpolar_pf_ws<float>(m, n, precision); break;
+    case MAK_C32: *bytes = rpolar_pf_ws<ccomplex>(m, n, precision); break;
+    default: return -1;
+  }
+  return 0;
+}
+
+#define MAK_RPOLPF(NAME, T, PT)                                                                 \
+  int NAME(int64_t m, int64_t n, const PT* dA, int64_t ldda, const PT* P, int64_t ldp,          \
+           const PT* Wh, int64_t ldwh, PT* dP, int64_t lddp, PT* dWh, int64_t lddwh,            \
+           const mak_pullback_opts* opts, void* work, size_t work_bytes, mak_info* info,        \
+           mak_stream_t stream) {                                                               \
+    return right_polar_pushforward_entry<T>(m, n, dA, ldda, P, ldp, Wh, ldwh, dP, lddp, dWh,    \
+                                            lddwh, opts, work, work_bytes, info, stream);       \
+  }
+MAK_RPOLPF(mak_right_polar_pushforward_d, double, double)
+MAK_RPOLPF(mak_right_polar_pushforward_z, zcomplex, void)
+MAK_RPOLPF(mak_right_polar_pushforward_s, float, float)
+MAK_RPOLPF(mak_right_polar_pushforward_c, ccomplex, void)
+
+#define MAK_POLPF(NAME, T, PT)                                                                  \
+  int NAME(int64_t m, int64_t n, const PT* dA, int64_t ldda, const PT* W, int64_t ldw,          \
+           const PT* P, int64_t ldp, PT* dW, int64_t lddw, PT* dP, int64_t lddp,                \
+           const mak_pullback_opts* opts, void* work, size_t work_bytes, mak_info* info,        \
+           mak_stream_t stream) {                                                               \
+    return polar_pushforward_entry<T>(m, n, dA, ldda, W, ldw, P, ldp, dW, lddw, dP, lddp, opts, \
+                                      work, work_bytes, info, stream);                         \
+  }
+MAK_POLPF(mak_left_polar_pushforward_d, double, double)
+MAK_POLPF(mak_left_polar_pushforward_z, zcomplex, void)
+MAK_POLPF(mak_left_polar_pushforward_s, float, float)
+MAK_POLPF(mak_left_polar_pushforward_c, ccomplex, void)
+
+#define MAK_RPOLPB(NAME, T, PT)                                                                 \
+  int NAME(int64_t m, int64_t n, PT* dA, int64_t ldda, const PT* P, int64_t ldp, const PT* Wh,  \
+           int64_t ldwh, const PT* dP, int64_t lddp, const PT* dWh, int64_t lddwh,              \
+           const mak_pullback_opts* opts, void* work, size_t work_bytes, mak_info* info,        \
+           mak_stream_t stream) {                                                               \
+    return right_polar_pullback_entry<T>(m, n, dA, ldda, P, ldp, Wh, ldwh, dP, lddp, dWh,       \
+                                         lddwh, opts, work, work_bytes, info, stream);          \
+  }
+MAK_RPOLPB(mak_right_polar_pullback_d, double, double)
+MAK_RPOLPB(mak_right_polar_pullback_z, zcomplex, void)
+MAK_RPOLPB(mak_right_polar_pullback_s, float, float)
+MAK_RPOLPB(mak_right_polar_pullback_c, ccomplex, void)
 
 }  // extern "C"

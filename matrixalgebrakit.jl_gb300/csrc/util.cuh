@@ -41,6 +41,41 @@ inline int set_identity(cudaStream_t st, int64_t m, int64_t n, T* B, int64_t ldb
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
 
+// B (n x m) = op(A)^H for A m x n, or B += A^H (ADD): 32 x 32 tiles through
+// shared memory so both the read of A and the write of B are coalesced
+template <class T, bool ADD>
+__global__ void __launch_bounds__(256) ctranspose_kernel(int64_t m, int64_t n,
+                                                         const T* __restrict__ A, int64_t lda,
+                                                         T* __restrict__ B, int64_t ldb) {
+  __shared__ T t[32][33];
+  const int64_t i0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t i = i0 + tx, j = j0 + r;
+    if (i < m && j < n) t[r][tx] = A[i + j * lda];  // t[j - j0][i - i0]
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t j = j0 + tx, i = i0 + r;  // B[j, i] = conj(A[i, j])
+    if (i < m && j < n) {
+      const T v = conj_(t[tx][r]);
+      if (ADD) B[j + i * ldb] += v;
+      else B[j + i * ldb] = v;
+    }
+  }
+}
+template <class T>
+inline int ctranspose(cudaStream_t st, int64_t m, int64_t n, const T* A, int64_t lda, T* B,
+                      int64_t ldb, bool add = false) {
+  if (m <= 0 || n <= 0) return 0;
+  if (ceil_div(n, 32) > 65535) return MAK_ERR_UNSUPPORTED;
+  dim3 g((unsigned)ceil_div(m, 32), (unsigned)ceil_div(n, 32));
+  note_launch();
+  if (add) ctranspose_kernel<T, true><<<g, 256, 0, st>>>(m, n, A, lda, B, ldb);
+  else ctranspose_kernel<T, false><<<g, 256, 0, st>>>(m, n, A, lda, B, ldb);
+  return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+}
+
 // ---- reductions -------------------------------------------------------------
 // Partial results per CTA, then one CTA folds them in a fixed order.
 constexpr int RED_CTAS = 304;

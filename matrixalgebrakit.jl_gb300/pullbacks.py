@@ -1,4 +1,5 @@
-"""Reverse rules: ``qr_pullback_`` and ``left_polar_pullback_`` on CUDA tensors.
+"""Reverse rules: ``qr_pullback_``, ``left_polar_pullback_`` and
+``right_polar_pullback_`` on CUDA tensors.
 
 Mirror ``qr_pullback!(ΔA, A, (Q, R), (ΔQ, ΔR); rank_atol, gauge_atol)``
 (src/pullbacks/qr.jl:73-120) and ``left_polar_pullback!(ΔA, A, (W, P),
@@ -8,7 +9,8 @@ returned; a cotangent given as ``None`` is a zero tangent
 cotangent emits the reference's warning (qr.jl:50-51).  These are the
 functions the package's ChainRulesCore and Mooncake rules call
 (ext/MatrixAlgebraKitChainRulesCoreExt.jl:34,254), so the Julia extension
-specialises exactly these two for CuMatrix.
+specialises these for CuMatrix.  The right polar rule (polar.jl:37-59) is
+the conjugate transpose of the left one.
 """
 
 from __future__ import annotations
@@ -110,6 +112,46 @@ def left_polar_pullback_(dA, A, WP, dWP, precision="native", _info=None):
         rc = fn(m, n, ptr(dA), ld_or_raise(dA, "dA"), ptr(W), ld_or_raise(W, "W"), ptr(P),
                 ld_or_raise(P, "P"), ptr(dW), ld_or_raise(dW, "dW") if dW is not None else 1,
                 ptr(dP), ld_or_raise(dP, "dP") if dP is not None else 1, ct.byref(opts),
+                ptr(work), nbytes.value, ptr(info), stream_handle(dev))
+        check_rc(rc, fn.__name__)
+        inf = read_info(info)
+    check_status(inf, fn.__name__)
+    if _info is not None:
+        _info.update(iterations=inf.iterations)
+    return dA
+
+
+def right_polar_pullback_(dA, A, PWh, dPWh, precision="native", _info=None):
+    """``right_polar_pullback!(ΔA, A, (P, Wᴴ), (ΔP, ΔWᴴ))`` (src/pullbacks/polar.jl:
+    37-59): dA += (pullback of right_polar at (P, Wh)).  On the device this is
+    the conjugate transpose of the left pullback of A^H at (Wh^H, P) with
+    cotangents (dWh^H, dP): the same Sylvester solve, transposed."""
+    P, Wh = PWh
+    dP, dWh = dPWh
+    check_cuda_tensor(dA, "dA")
+    m, n = Wh.shape
+    if n < m:
+        raise ArgumentError(f"Wh must have at least as many columns ({n}) as rows ({m})")
+    if tuple(dA.shape) != (m, n):
+        raise DimensionMismatch(f"dA must have size {(m, n)}")
+    _chk(P, (m, m), dA.dtype, "P")
+    _chk(Wh, (m, n), dA.dtype, "Wh")
+    _chk(dP, (m, m), dA.dtype, "dP")
+    _chk(dWh, (m, n), dA.dtype, "dWh")
+    opts = _opts(None, None, precision)
+    L = lib()
+    nbytes = ct.c_size_t(0)
+    check_rc(L.mak_right_polar_pullback_workspace(DTYPE_CODE[dA.dtype], m, n, opts.precision,
+                                                  ct.byref(nbytes)),
+             "mak_right_polar_pullback_workspace")
+    dev = dA.device
+    with torch.cuda.device(dev):
+        work = workspace(nbytes.value, dev)
+        info = new_info(dev)
+        fn = getattr(L, f"mak_right_polar_pullback_{SUFFIX[dA.dtype]}")
+        rc = fn(m, n, ptr(dA), ld_or_raise(dA, "dA"), ptr(P), ld_or_raise(P, "P"), ptr(Wh),
+                ld_or_raise(Wh, "Wh"), ptr(dP), ld_or_raise(dP, "dP") if dP is not None else 1,
+                ptr(dWh), ld_or_raise(dWh, "dWh") if dWh is not None else 1, ct.byref(opts),
                 ptr(work), nbytes.value, ptr(info), stream_handle(dev))
         check_rc(rc, fn.__name__)
         inf = read_info(info)

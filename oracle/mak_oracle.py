@@ -22,6 +22,9 @@ __all__ = [
     "gaussian", "haar", "polar_test_matrix", "rank_deficient", "batched_blocks",
     "qr_residual", "orth_error", "rel_err", "qr_flops", "polar_flops",
     "is_complex", "real_dtype", "eps",
+    "lq_via_qr", "lq_compact", "lq_full", "lq_householder_native", "right_polar_newton",
+    "right_polar_svd", "right_polar_pullback", "left_polar_pushforward",
+    "right_polar_pushforward",
 ]
 
 
@@ -140,6 +143,87 @@ def qr_null(A, positive: bool = True):
     return np.asfortranarray(Q[:, min(m, n):])
 
 
+# --------------------------------------------------------------------- LQ ---
+
+def lq_via_qr(A, full: bool = False, positive: bool = True, blocksize: int = 0):
+    """``lq_via_qr!(A, L, Q, qr_alg)`` (src/implementations/lq.jl:303-318), the
+    LQ the reference computes for its GPU drivers (lq.jl:130-131) and for
+    ``LQViaTransposedQR`` (src/interface/decompositions.jl:340-353): the QR of
+    ``A^H`` (``qr_full!`` when Q is n x n, else ``qr_compact!``), then
+    ``Q = Qt^H`` and ``L = Rt^H``.  Returns ``(L, Q)``: compact L m x min(m,n),
+    Q min(m,n) x n; full L m x n, Q n x n."""
+    A = np.asarray(A)
+    At = np.asfortranarray(A.conj().T)
+    Qt, Rt = (qr_full if full else qr_compact)(At, positive=positive, blocksize=blocksize)
+    return np.asfortranarray(Rt.conj().T), np.asfortranarray(Qt.conj().T)
+
+
+def lq_compact(A, positive: bool = True, blocksize: int = 0):
+    """``lq_compact!`` through the transposed QR (see ``lq_via_qr``)."""
+    return lq_via_qr(A, full=False, positive=positive, blocksize=blocksize)
+
+
+def lq_full(A, positive: bool = True, blocksize: int = 0):
+    """``lq_full!`` through the transposed QR (see ``lq_via_qr``)."""
+    return lq_via_qr(A, full=True, positive=positive, blocksize=blocksize)
+
+
+def _householder_vec(v):
+    """``_householder!(v, 1)`` (src/common/householder.jl:35-67): returns
+    ``(beta, v, nu)`` with ``v[0] = 1`` so that ``(I - beta v v^H) x = nu e_1``
+    for the input x (nu = ||x|| >= 0)."""
+    v = np.array(v, copy=True)
+    sigma = float(np.sum(np.abs(v[1:]) ** 2))
+    vi = v[0]
+    nu = math.sqrt(abs(vi) ** 2 + sigma)
+    if sigma == 0 and vi == nu:
+        return v.dtype.type(0), v, nu
+    if vi.real < 0:
+        vi = vi - nu
+    else:
+        vi = ((vi - np.conj(vi)) * nu - sigma) / (np.conj(vi) + nu)
+    v[1:] = v[1:] / vi
+    v[0] = 1
+    beta = -np.conj(vi) / nu
+    return beta, v, nu
+
+
+def lq_householder_native(A, full: bool = False):
+    """``lq_householder!(::Native, A, L, Q)`` (src/implementations/lq.jl:
+    177-219): unblocked Householder LQ, one reflector per row from
+    ``_householder!(conj(A[i, i:n]))``, applied from the right to the rows
+    below; Q accumulated backwards from ``one!(Q)``.  diag(L) = nu >= 0, so
+    this is the positive gauge.  Pure-Python loop over rows: small cases only."""
+    A = np.array(A, copy=True)
+    if not np.issubdtype(A.dtype, np.inexact):
+        A = A.astype(np.float64)
+    m, n = A.shape
+    k = min(m, n)
+    lcols = n if full else k
+    qrows = n if full else k
+    L = np.zeros((m, lcols), dtype=A.dtype)
+    refl = []
+    for i in range(k):
+        L[i, :i] = A[i, :i]
+        beta, v, nu = _householder_vec(np.conj(A[i, i:]))
+        L[i, i] = nu
+        if i + 1 < m:
+            B = A[i + 1:, i:]
+            # rmul!(A, H) with H = HouseholderReflection(conj(beta), v): A (I - conj(beta) v v^H)
+            A[i + 1:, i:] = B - np.conj(beta) * np.outer(B @ v, v.conj())
+        refl.append((beta, v))
+    if m > k:
+        L[k:, :k] = A[k:, :k]
+    Q = np.zeros((qrows, n), dtype=A.dtype)
+    Q[np.arange(qrows), np.arange(qrows)] = 1
+    for i in range(k - 1, -1, -1):
+        beta, v = refl[i]
+        # rmul!(Q, H^H) with H^H = I - beta v v^H
+        Qi = Q[:, i:]
+        Q[:, i:] = Qi - beta * np.outer(Qi @ v, v.conj())
+    return np.asfortranarray(L), np.asfortranarray(Q)
+
+
 # ----------------------------------------------------------------- polar ---
 
 def project_hermitian(A):
@@ -233,6 +317,63 @@ def left_polar_newton(A, tol: float | None = None, maxiter: int = 10,
     W = np.asfortranarray(W.astype(dtype, copy=False))
     P = project_hermitian(W.conj().T @ A0) if compute_p else None
     return W, P, {"iterations": it, "residual": conv, "converged": conv <= tol}
+
+
+def right_polar_newton(A, tol: float | None = None, maxiter: int = 10,
+                       compute_p: bool = True):
+    """``right_polar!(A, (P, Wh), PolarNewton(; tol, maxiter))``
+    (src/implementations/polar.jl:113-125) with ``right_polar_newton!``
+    (polar.jl:168-206): for m < n an initial LQ, then the scaled Newton
+    iteration on the lower-triangular (or square) factor; ``Wh = Lc Q`` and
+    ``P = project_hermitian(A Wh^H)``.  Returns ``(P, Wh, info)``."""
+    A0 = np.array(A, order="F", copy=True)
+    dtype = A0.dtype
+    m, n = A0.shape
+    if n < m:
+        raise ValueError(f"input matrix needs at least as many columns ({n}) as rows ({m})")
+    if tol is None:
+        tol = defaulttol(dtype)
+    eye = np.eye(m, dtype=dtype)
+    if m < n:
+        Lf, Q = lq_compact(A0)
+        X = Lf.copy()
+        # ldiv!(LowerTriangular(Lc)', one!(Linvh)) = L^{-H}
+        Xinvh = sla.solve_triangular(Lf, eye, trans="C", lower=True)
+    else:
+        Q = None
+        X = A0.copy()
+        Xinvh = sla.lu_solve(sla.lu_factor(X), eye, trans=2)
+    gamma = math.sqrt(np.linalg.norm(Xinvh) / np.linalg.norm(X))
+    X = X * gamma
+    Xinvh = Xinvh / gamma
+    X, Xinvh = (X + Xinvh) / 2, Xinvh - X
+    it = 1
+    conv = float(np.max(np.abs(Xinvh))) if Xinvh.size else 0.0
+    while it < maxiter and conv > tol:
+        Xinvh = sla.lu_solve(sla.lu_factor(X), eye, trans=2)
+        gamma = math.sqrt(np.linalg.norm(Xinvh) / np.linalg.norm(X))
+        X = X * gamma
+        Xinvh = Xinvh / gamma
+        X, Xinvh = (X + Xinvh) / 2, Xinvh - X
+        conv = float(np.max(np.abs(Xinvh)))
+        it += 1
+    Wh = X @ Q if m < n else X
+    Wh = np.asfortranarray(Wh.astype(dtype, copy=False))
+    P = project_hermitian(A0 @ Wh.conj().T) if compute_p else None
+    return P, Wh, {"iterations": it, "residual": conv, "converged": conv <= tol}
+
+
+def right_polar_svd(A):
+    """``right_polar!(A, (P, Wh), PolarViaSVD(...))`` (src/implementations/
+    polar.jl:71-83): ``Wh = U Vh`` and ``P = (U sqrt(S)) (U sqrt(S))^H``."""
+    A = np.asarray(A)
+    m, n = A.shape
+    if n < m:
+        raise ValueError(f"input matrix needs at least as many columns ({n}) as rows ({m})")
+    U, S, Vh = svd_compact(A)
+    US = U * np.sqrt(S)[None, :]
+    return np.asfortranarray((US @ US.conj().T).astype(A.dtype, copy=False)), \
+        np.asfortranarray(U @ Vh)
 
 
 # ------------------------------------------------------------- pullbacks ---
@@ -376,6 +517,60 @@ def left_polar_pullback(dA, A, W, P, dW, dP):
         dWP = dWP - W @ (W.conj().T @ dWP)
         dA += dWP
     return dA
+
+
+def right_polar_pullback(dA, A, P, Wh, dP, dWh):
+    """``right_polar_pullback!(dA, A, (P, Wh), (dP, dWh))`` (src/pullbacks/
+    polar.jl:37-59).  ``dP``/``dWh`` may be ``None`` (a zero tangent)."""
+    dA = np.array(dA, order="F", copy=True)
+    P = np.asarray(P)
+    Wh = np.asarray(Wh)
+    if dP is not None:
+        dP = project_hermitian(dP)
+    M = np.zeros_like(P)
+    if dWh is not None:
+        M = M + np.asarray(dWh) @ Wh.conj().T
+    if dP is not None:
+        M = M - P @ dP
+    C = sylvester(P, P, M.conj().T - M)
+    if dP is not None:
+        C = C + dP
+    dA += C @ Wh
+    if dWh is not None:
+        PdWh = np.linalg.solve(P, np.asarray(dWh))
+        PdWh = PdWh - (PdWh @ Wh.conj().T) @ Wh
+        dA += PdWh
+    return dA
+
+
+def left_polar_pushforward(dA, A, W, P):
+    """``left_polar_pushforward!(dA, A, (W, P), (dW, dP))`` (src/pushforwards/
+    polar.jl:1-12): returns ``(dW, dP)``."""
+    dA = np.asarray(dA)
+    W = np.asarray(W)
+    P = np.asarray(P)
+    dP = W.conj().T @ dA
+    K = sylvester(P, P, dP.conj().T - dP)
+    dW = dA @ np.linalg.inv(P)
+    dW = dW - W @ (W.conj().T @ dW)
+    dW = dW + W @ K
+    dP = dP - K @ P
+    return np.asfortranarray(dW), np.asfortranarray(dP)
+
+
+def right_polar_pushforward(dA, A, P, Wh):
+    """``right_polar_pushforward!(dA, A, (P, Wh), (dP, dWh))`` (src/pushforwards/
+    polar.jl:14-26): returns ``(dWh, dP)`` in the reference's order."""
+    dA = np.asarray(dA)
+    P = np.asarray(P)
+    Wh = np.asarray(Wh)
+    dP = dA @ Wh.conj().T
+    K = sylvester(P, P, dP.conj().T - dP)
+    dWh = np.linalg.inv(P) @ dA
+    dWh = dWh - (dWh @ Wh.conj().T) @ Wh
+    dWh = dWh + K @ Wh
+    dP = dP - P @ K
+    return np.asfortranarray(dWh), np.asfortranarray(dP)
 
 
 # ------------------------------------------------------------ generators ---

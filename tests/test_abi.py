@@ -98,3 +98,64 @@ def test_algorithm_selection(mak):
         GB300_HouseholderQR(pivoted=True)
     with pytest.raises(ArgumentError):
         select_algorithm("qr_compact_", None, "NoSuchAlgorithm")
+
+
+def test_dual_entry_points_validate_on_host(mak):
+    """LQ, right polar, the right pullback and the pushforwards: workspace
+    queries and argument checks run without a GPU (LAPACK -i codes)."""
+    from mak_gb300 import _lib
+
+    lib = mak.library()
+    nb = C.c_size_t(0)
+    qo = _lib.mak_qr_opts(1, 0, 0, 0)
+    po = _lib.mak_polar_opts(10, 0, 0.0)
+    pb = _lib.mak_pullback_opts(-1.0, -1.0, 0, 0)
+    for full in (0, 1):
+        assert lib.mak_lq_workspace(_lib.MAK_C64, 300, 700, full, C.byref(qo), C.byref(nb)) == 0
+        assert nb.value > 0
+    assert lib.mak_lq_workspace(_lib.MAK_F64, -1, 7, 0, C.byref(qo), C.byref(nb)) == -2
+    assert lib.mak_right_polar_workspace(_lib.MAK_F64, 30, 70, 1, C.byref(po), C.byref(nb)) == 0
+    assert nb.value > 0
+    assert lib.mak_right_polar_workspace(_lib.MAK_F64, 70, 30, 1, C.byref(po), C.byref(nb)) == -3
+    for fn in ("mak_right_polar_pullback_workspace", "mak_right_polar_pushforward_workspace"):
+        assert getattr(lib, fn)(_lib.MAK_C64, 20, 50, 0, C.byref(nb)) == 0 and nb.value > 0
+        assert getattr(lib, fn)(_lib.MAK_F64, 50, 20, 0, C.byref(nb)) == -3
+    assert lib.mak_left_polar_pushforward_workspace(_lib.MAK_F64, 50, 20, 1, C.byref(nb)) == 0
+    assert lib.mak_left_polar_pushforward_workspace(_lib.MAK_F64, 20, 50, 0, C.byref(nb)) == -3
+
+    rc = lib.mak_lq_compact_d(-1, 4, None, 4, None, 4, None, 4, C.byref(qo), None, 0, None, None)
+    assert rc == -1
+    rc = lib.mak_lq_compact_d(8, 4, 16, 4, None, 8, 32, 4, C.byref(qo), None, 0, None, None)
+    assert rc == -4  # lda < m
+    rc = lib.mak_lq_full_d(4, 8, 16, 4, None, 4, 32, 4, C.byref(qo), None, 0, None, None)
+    assert rc == -8  # ldq < n for the n x n Q
+    rc = lib.mak_right_polar_newton_d(8, 4, 16, 8, None, 8, 32, 8, C.byref(po), None, 0, None,
+                                      None)
+    assert rc == -2  # n >= m required
+    bad = _lib.mak_polar_opts(0, 0, 0.0)
+    rc = lib.mak_right_polar_newton_d(4, 8, 16, 4, None, 4, 32, 4, C.byref(bad), None, 0, None,
+                                      None)
+    assert rc == -9
+    rc = lib.mak_right_polar_pullback_d(8, 4, 16, 8, 32, 8, 48, 8, None, 8, None, 8, C.byref(pb),
+                                        None, 0, None, None)
+    assert rc == -2
+    rc = lib.mak_left_polar_pushforward_d(8, 4, 16, 8, 32, 8, 48, 4, None, 8, 64, 4, C.byref(pb),
+                                          None, 0, None, None)
+    assert rc == -9  # dW missing
+    rc = lib.mak_right_polar_pushforward_d(4, 8, 16, 4, 32, 4, 48, 4, 64, 4, 80, 2, C.byref(pb),
+                                           None, 0, None, None)
+    assert rc == -12  # lddwh < m
+    rc = lib.mak_lq_compact_z(4, 8, 16, 4, None, 4, 32, 4, C.byref(qo), None, 0, None, None)
+    assert rc == -12  # info missing (checked before the workspace)
+
+
+def test_dual_algorithm_selection(mak):
+    from mak_gb300 import (GB300_HouseholderQR, GB300_PolarNewton, LQViaTransposedQR,
+                           default_algorithm, select_algorithm)
+
+    assert default_algorithm("lq_compact_") == LQViaTransposedQR(GB300_HouseholderQR())
+    assert default_algorithm("right_polar") == GB300_PolarNewton()
+    alg = select_algorithm("lq_full_", None, GB300_HouseholderQR(blocksize=8))
+    assert isinstance(alg, LQViaTransposedQR) and alg.alg.blocksize == 8
+    assert select_algorithm("lq_compact", None, None, positive=False).positive is False
+    assert select_algorithm("qr_compact_", None, GB300_HouseholderQR()) == GB300_HouseholderQR()

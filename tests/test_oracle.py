@@ -155,3 +155,125 @@ def test_oracle_polar_pullback_fd(dt):
 def test_oracle_flop_counts():
     assert abs(O.qr_flops(512, 256) - 0.1118e9) / 0.1118e9 < 1e-3
     assert abs(O.qr_flops(16384, 8192) - 3.665e12) / 3.665e12 < 1e-3
+
+
+# ----------------------------------------------- LQ, right polar, pushforwards ---
+
+@pytest.mark.parametrize("path", sorted(GOLD.glob("qr_kat_*.npz")), ids=lambda p: p.stem)
+def test_oracle_lq_known_answer(path):
+    """A^H = R0^H Q0^H is the positive-diagonal LQ of A^H (the QR known
+    answers, conjugate-transposed); both LQ routes must return it."""
+    d = np.load(path)
+    Ah = d["A"].conj().T
+    for L, Q in (O.lq_compact(Ah), O.lq_householder_native(Ah)):
+        assert O.rel_err(L, d["R"].conj().T) < 1e-12
+        assert O.rel_err(Q, d["Q"].conj().T) < 1e-12
+
+
+@pytest.mark.parametrize("dt", DTYPES)
+@pytest.mark.parametrize("shape", [(37, 54), (54, 54), (54, 37), (1, 9)])
+def test_oracle_lq_properties(dt, shape):
+    """test/testsuite/decompositions/lq.jl:21-160: L Q = A, Q has orthonormal
+    rows (unitary for lq_full), L lower triangular with a positive diagonal;
+    the transposed-QR route agrees with the native row-Householder LQ."""
+    rng = np.random.default_rng(321)
+    m, n = shape
+    A = O.gaussian(rng, m, n, dt)
+    k = min(m, n)
+    for full in (False, True):
+        L, Q = (O.lq_full if full else O.lq_compact)(A)
+        assert L.shape == ((m, n) if full else (m, k))
+        assert Q.shape == ((n, n) if full else (k, n))
+        assert O.qr_residual(A.T, Q.T, L.T) < prec(dt)
+        assert O.orth_error(Q.conj().T) < prec(dt) * np.sqrt(Q.shape[0])
+        assert np.allclose(L, np.tril(L))
+        dg = np.diagonal(L)
+        assert np.all(dg.real >= 0) and np.all(np.abs(dg.imag) == 0)
+        Ln, Qn = O.lq_householder_native(A, full=full)
+        tol = 1e-11 if O.eps(dt) < 1e-10 else 1e-4
+        assert O.rel_err(Ln, L) < tol
+        assert O.rel_err(Qn[:k], Q[:k]) < tol
+
+
+@pytest.mark.parametrize("path", sorted(GOLD.glob("polar_kat_*.npz")), ids=lambda p: p.stem)
+def test_oracle_right_polar_known_answer(path):
+    """A^H = P W^H: the right polar factors of A^H are the left factors of A,
+    conjugate-transposed."""
+    d = np.load(path)
+    Ah = d["A"].conj().T
+    for P, Wh in (O.right_polar_svd(Ah), O.right_polar_newton(Ah)[:2]):
+        assert O.rel_err(Wh, d["W"].conj().T) < 1e-11
+        assert O.rel_err(P, d["P"]) < 1e-11
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_right_polar_newton_vs_svd(dt):
+    """test/testsuite/decompositions/polar.jl:47-80."""
+    rng = np.random.default_rng(6)
+    for (m, n) in ((37, 54), (54, 54), (40, 120)):
+        A = O.gaussian(rng, m, n, dt)
+        P1, Wh1 = O.right_polar_svd(A)
+        P2, Wh2, info = O.right_polar_newton(A)
+        assert info["converged"]
+        assert O.rel_err(Wh1, Wh2) < 1e-12 and O.rel_err(P1, P2) < 1e-12
+        assert O.orth_error(Wh2.conj().T) < 1e-13 * m
+        assert np.linalg.norm(A - P2 @ Wh2) / np.linalg.norm(A) < 1e-13
+    with pytest.raises(ValueError):
+        O.right_polar_newton(O.gaussian(rng, 5, 4, dt))
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_right_polar_pullback_fd(dt):
+    """Central finite differences of Re<dP, P(A)> + Re<dWh, Wh(A)>, and the
+    conjugate-transpose identity with the left pullback of A^H."""
+    rng = np.random.default_rng(14)
+    A = O.gaussian(rng, 17, 19, dt)
+    P, Wh = O.right_polar_svd(A)
+    dP, dWh = O.gaussian(rng, 17, 17, dt), O.gaussian(rng, 17, 19, dt)
+    dA = O.right_polar_pullback(np.zeros_like(A), A, P, Wh, dP, dWh)
+    E = O.gaussian(rng, 17, 19, dt)
+
+    def loss(X):
+        Px, Whx = O.right_polar_svd(X)
+        return np.real(np.vdot(dP, Px) + np.vdot(dWh, Whx))
+
+    fd = _fd(loss, A, E)
+    assert abs(fd - np.real(np.vdot(dA, E))) < 1e-7 * max(1, abs(fd))
+    dAt = O.left_polar_pullback(np.zeros_like(A.T), A.conj().T, Wh.conj().T, P,
+                                dWh.conj().T, dP)
+    assert O.rel_err(dAt.conj().T, dA) < 1e-12
+    for zdP, zdWh in ((None, dWh), (dP, None)):
+        d1 = O.right_polar_pullback(np.zeros_like(A), A, P, Wh, zdP, zdWh)
+        d2 = O.right_polar_pullback(np.zeros_like(A), A, P, Wh,
+                                    np.zeros_like(dP) if zdP is None else zdP,
+                                    np.zeros_like(dWh) if zdWh is None else zdWh)
+        assert O.rel_err(d1, d2) < 1e-13
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_polar_pushforward_fd(dt):
+    """Both pushforwards against central differences of the SVD-based polar
+    decomposition, and the pairing <dA_pullback, E> = <cotangent, tangent>."""
+    rng = np.random.default_rng(15)
+    A = O.gaussian(rng, 19, 17, dt)
+    E = O.gaussian(rng, 19, 17, dt)
+    W, P = O.left_polar_svd(A)
+    dW, dP = O.left_polar_pushforward(E, A, W, P)
+    fW = _fd(lambda X: O.left_polar_svd(X)[0], A, E)
+    fP = _fd(lambda X: O.left_polar_svd(X)[1], A, E)
+    assert O.rel_err(dW, fW) < 1e-7 and O.rel_err(dP, fP) < 1e-7
+    cW, cP = O.gaussian(rng, 19, 17, dt), O.project_hermitian(O.gaussian(rng, 17, 17, dt))
+    dA = O.left_polar_pullback(np.zeros_like(A), A, W, P, cW, cP)
+    lhs = np.real(np.vdot(dA, E))
+    rhs = np.real(np.vdot(cW, dW) + np.vdot(cP, dP))
+    assert abs(lhs - rhs) < 1e-10 * max(1, abs(lhs))
+
+    B = A.conj().T.copy()
+    F = E.conj().T.copy()
+    Pb, Whb = O.right_polar_svd(B)
+    dWh, dPb = O.right_polar_pushforward(F, B, Pb, Whb)
+    fWh = _fd(lambda X: O.right_polar_svd(X)[1], B, F)
+    fPb = _fd(lambda X: O.right_polar_svd(X)[0], B, F)
+    assert O.rel_err(dWh, fWh) < 1e-7 and O.rel_err(dPb, fPb) < 1e-7
+    # conjugate-transpose duality: right pushforward of A^H = (left pushforward of A)^H
+    assert O.rel_err(dWh, dW.conj().T) < 1e-12 and O.rel_err(dPb, dP.conj().T) < 1e-12
