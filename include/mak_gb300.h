@@ -457,6 +457,81 @@ int mak_right_polar_pushforward_c(int64_t m, int64_t n, const void* dA, int64_t 
                                   const mak_pullback_opts* opts, void* work, size_t work_bytes,
                                   mak_info* info, mak_stream_t stream);
 
+/* qr_null_pullback!(dA, A, N, dN; gauge_atol)
+ * Replaces the reference's qr_null_pullback! (src/pullbacks/qr.jl:141-152)
+ * for N = qr_null(A) (m x (m - min(m,n))): with a nonzero dN,
+ * X = (dN^H Q) R^{-H} from qr_compact(A; positive = true) on the device, and
+ * dA -= N X.  The gauge ||antiherm(N^H dN)||_F goes to info->gauge against
+ * info->gauge_atol (opts->gauge_atol < 0: eps(max|dN|)^(3/4)); the caller
+ * warns.  A is read, not written.  dN may be NULL (nothing to add).
+ */
+int mak_qr_null_pullback_workspace(int dtype, int64_t m, int64_t n, int precision, size_t* bytes);
+int mak_qr_null_pullback_d(int64_t m, int64_t n, double* dA, int64_t ldda, const double* A,
+                           int64_t lda, const double* N, int64_t ldn, const double* dN,
+                           int64_t lddn, const mak_pullback_opts* opts, void* work,
+                           size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_qr_null_pullback_z(int64_t m, int64_t n, void* dA, int64_t ldda, const void* A,
+                           int64_t lda, const void* N, int64_t ldn, const void* dN, int64_t lddn,
+                           const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                           mak_info* info, mak_stream_t stream);
+int mak_qr_null_pullback_s(int64_t m, int64_t n, float* dA, int64_t ldda, const float* A,
+                           int64_t lda, const float* N, int64_t ldn, const float* dN,
+                           int64_t lddn, const mak_pullback_opts* opts, void* work,
+                           size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_qr_null_pullback_c(int64_t m, int64_t n, void* dA, int64_t ldda, const void* A,
+                           int64_t lda, const void* N, int64_t ldn, const void* dN, int64_t lddn,
+                           const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                           mak_info* info, mak_stream_t stream);
+
+/* lq_pullback!(dA, A, (L, Q), (dL, dQ); rank_atol, gauge_atol)
+ * Replaces the reference's lq_pullback! (src/pullbacks/lq.jl:71-112), as the
+ * conjugate transpose of qr_pullback! of A^H at (Q^H, L^H) with (dQ^H, dL^H).
+ * full = 1 for lq_full output (Q n x n, L m x n; only differs when n > m).
+ * dA accumulated into; dL / dQ may be NULL.  Same info fields as
+ * mak_qr_pullback_*.
+ */
+int mak_lq_pullback_workspace(int dtype, int64_t m, int64_t n, int full, int precision,
+                              size_t* bytes);
+int mak_lq_pullback_d(int64_t m, int64_t n, int full, double* dA, int64_t ldda, const double* L,
+                      int64_t ldl, const double* Q, int64_t ldq, const double* dL, int64_t lddl,
+                      const double* dQ, int64_t lddq, const mak_pullback_opts* opts, void* work,
+                      size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_pullback_z(int64_t m, int64_t n, int full, void* dA, int64_t ldda, const void* L,
+                      int64_t ldl, const void* Q, int64_t ldq, const void* dL, int64_t lddl,
+                      const void* dQ, int64_t lddq, const mak_pullback_opts* opts, void* work,
+                      size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_pullback_s(int64_t m, int64_t n, int full, float* dA, int64_t ldda, const float* L,
+                      int64_t ldl, const float* Q, int64_t ldq, const float* dL, int64_t lddl,
+                      const float* dQ, int64_t lddq, const mak_pullback_opts* opts, void* work,
+                      size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_pullback_c(int64_t m, int64_t n, int full, void* dA, int64_t ldda, const void* L,
+                      int64_t ldl, const void* Q, int64_t ldq, const void* dL, int64_t lddl,
+                      const void* dQ, int64_t lddq, const mak_pullback_opts* opts, void* work,
+                      size_t work_bytes, mak_info* info, mak_stream_t stream);
+
+/* lq_null_pullback!(dA, A, Nh, dNh; gauge_atol)
+ * Replaces the reference's lq_null_pullback! (src/pullbacks/lq.jl:133-145)
+ * for Nh = lq_null(A) ((n - min(m,n)) x n): X = L^{-H} Q dNh^H, dA -= X Nh,
+ * as the conjugate transpose of the QR null-space rule on A^H.
+ */
+int mak_lq_null_pullback_workspace(int dtype, int64_t m, int64_t n, int precision, size_t* bytes);
+int mak_lq_null_pullback_d(int64_t m, int64_t n, double* dA, int64_t ldda, const double* A,
+                           int64_t lda, const double* Nh, int64_t ldnh, const double* dNh,
+                           int64_t lddnh, const mak_pullback_opts* opts, void* work,
+                           size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_null_pullback_z(int64_t m, int64_t n, void* dA, int64_t ldda, const void* A,
+                           int64_t lda, const void* Nh, int64_t ldnh, const void* dNh,
+                           int64_t lddnh, const mak_pullback_opts* opts, void* work,
+                           size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_null_pullback_s(int64_t m, int64_t n, float* dA, int64_t ldda, const float* A,
+                           int64_t lda, const float* Nh, int64_t ldnh, const float* dNh,
+                           int64_t lddnh, const mak_pullback_opts* opts, void* work,
+                           size_t work_bytes, mak_info* info, mak_stream_t stream);
+int mak_lq_null_pullback_c(int64_t m, int64_t n, void* dA, int64_t ldda, const void* A,
+                           int64_t lda, const void* Nh, int64_t ldnh, const void* dNh,
+                           int64_t lddnh, const mak_pullback_opts* opts, void* work,
+                           size_t work_bytes, mak_info* info, mak_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

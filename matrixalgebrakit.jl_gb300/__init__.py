@@ -41,10 +41,12 @@ def library():
     """The loaded ctypes handle of libmak_gb300.so (raises if unavailable)."""
     return _lib.load()
 
-from .pullbacks import left_polar_pullback_, qr_pullback_, right_polar_pullback_  # noqa: E402
+from .pullbacks import (left_polar_pullback_, lq_null_pullback_, lq_pullback_,  # noqa: E402
+                        qr_null_pullback_, qr_pullback_, right_polar_pullback_)
 from .pushforwards import left_polar_pushforward_, right_polar_pushforward_  # noqa: E402
 
-__all__ += ["qr_pullback_", "left_polar_pullback_", "right_polar_pullback_",
+__all__ += ["qr_pullback_", "left_polar_pullback_", "right_polar_pullback_", "qr_null_pullback_",
+            "lq_pullback_", "lq_null_pullback_",
             "left_polar_pushforward_", "right_polar_pushforward_"]
 
 from .batched import batched_left_polar, batched_qr_compact  # noqa: E402

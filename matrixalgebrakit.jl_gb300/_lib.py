@@ -110,6 +110,18 @@ for _s in "dzsc":
     SIGNATURES[f"mak_right_polar_pullback_{_s}"] = (C.c_int, _PB_ARGS)
     SIGNATURES[f"mak_left_polar_pushforward_{_s}"] = (C.c_int, _PB_ARGS)
     SIGNATURES[f"mak_right_polar_pushforward_{_s}"] = (C.c_int, _PB_ARGS)
+# null-space pullbacks and the LQ pullback
+_NULLPB_ARGS = [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, C.POINTER(mak_pullback_opts),
+                _p, _sz, _p, _p]
+for _nm in ("qr_null", "lq_null"):
+    SIGNATURES[f"mak_{_nm}_pullback_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
+                                                             C.POINTER(_sz)])
+    for _s in "dzsc":
+        SIGNATURES[f"mak_{_nm}_pullback_{_s}"] = (C.c_int, _NULLPB_ARGS)
+SIGNATURES["mak_lq_pullback_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int, C.c_int,
+                                                     C.POINTER(_sz)])
+for _s in "dzsc":
+    SIGNATURES[f"mak_lq_pullback_{_s}"] = SIGNATURES[f"mak_qr_pullback_{_s}"]
 SIGNATURES["mak_right_polar_pushforward_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
                                                                  C.POINTER(_sz)])
 

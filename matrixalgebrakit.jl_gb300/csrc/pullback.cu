@@ -790,6 +790,320 @@ static size_t rpolar_pb_ws(int64_t m, int64_t n, int prec) {
   return meas.off + 256;
 }
 
+// ------------------------------------------------ null-space and LQ pullbacks --
+template <class R>
+__global__ void sqrt_scalar_kernel(const R* x, R* out) {
+  *out = sqrt(*x);
+}
+
+// qr_null_pullback! (reference src/pullbacks/qr.jl:141-152) for N = qr_null(A)
+// (m x (m-n), nonempty only for m > n) and a nonzero cotangent dN:
+//   gauge = ||(S - S^H)/2||_F with S = N^H dN (check_qr_null_cotangents,
+//   qr.jl:122-128; reported in info->gauge against info->gauge_atol),
+//   Q, R = qr_compact(A; positive = true),  X = (dN^H Q) R^{-H},  dA -= N X.
+// R^{-1} is the explicit Gauss-Jordan inverse of the triangular factor (no
+// pivot exchanges occur on a triangular matrix).  A is read, not written.
+template <class T>
+static int qr_null_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldda,
+                                const T* A, int64_t lda, const T* N, int64_t ldn, const T* dN,
+                                int64_t lddn, double gauge_atol, int precision, Arena& ar,
+                                mak_info* info) {
+  using Rr = real_t<T>;
+  const int64_t k = m < n ? m : n;
+  const int64_t nc = m - k;
+  Rr* scal = ar.take<Rr>(RED_CTAS + 16);
+  T* Ac = ar.take<T>((size_t)m * n + 1);
+  T* Qc = ar.take<T>((size_t)m * k + 1);
+  T* Rc = ar.take<T>((size_t)k * k + 1);  // R is k x n = k x k whenever nc > 0
+  T* S = ar.take<T>((size_t)nc * nc + 1);
+  T* Sa = ar.take<T>((size_t)nc * nc + 1);
+  T* G1 = ar.take<T>((size_t)nc * k + 1);
+  T* X = ar.take<T>((size_t)nc * k + 1);
+  T* Rinv = ar.take<T>((size_t)k * k + 1);
+  int* iperm = ar.take<int>(k + 1);
+  size_t tail_bytes = 0;
+  {
+    Arena mq(nullptr, 0);
+    qr_run<T>(st, m, n, nullptr, m > 0 ? m : 1, nullptr, m > 0 ? m : 1, k, nullptr,
+              k > 0 ? k : 1, k, 1, 0, precision, mq, nullptr);
+    tail_bytes = mq.off + 256;
+    Arena mg(nullptr, 0);
+    gje_inverse<T>(st, k, nullptr, k > 0 ? k : 1, nullptr, precision, mg, nullptr);
+    if (mg.off + 256 > tail_bytes) tail_bytes = mg.off + 256;
+    const int64_t shapes[4][3] = {{nc, nc, m}, {nc, k, m}, {nc, k, k}, {m, k, nc}};
+    for (auto& sh : shapes) {
+      Arena m2(nullptr, 0);
+      gemm_prec<T>(st, precision, sh[0], sh[1], sh[2], one_<T>(), opnd<T>(nullptr, 1),
+                   opnd<T>(nullptr, 1), zero_<T>(), nullptr, 1, m2, nullptr);
+      if (m2.off + 256 > tail_bytes) tail_bytes = m2.off + 256;
+    }
+  }
+  char* tail = ar.take<char>(tail_bytes);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  int* status = &info->status;
+  Rr* red = scal;
+  Rr* gauge = scal + RED_CTAS;
+  Rr* gatol = scal + RED_CTAS + 1;
+  Rr* tmp = scal + RED_CTAS + 2;
+  auto G = [&](int64_t M_, int64_t N_, int64_t K_, T alpha, Operand<T> a, Operand<T> b, T beta,
+               T* C_, int64_t ldc) -> int {
+    Arena oz(tail, tail_bytes);
+    return gemm_prec<T>(st, precision, M_, N_, K_, alpha, a, b, beta, C_, ldc, oz, status);
+  };
+  MAK_CUDA_TRY(cudaMemsetAsync(scal + RED_CTAS, 0, 16 * sizeof(Rr), st));
+  if (dN != nullptr && nc > 0) {
+    // gauge check of the cotangent
+    MAK_TRY(G(nc, nc, m, one_<T>(), opnd<T>(N, ldn, OP_C), opnd<T>(dN, lddn), zero_<T>(), S, nc));
+    {
+      dim3 g((unsigned)ceil_div(nc, 32), (unsigned)ceil_div(nc, 32));
+      note_launch();
+      antiherm_kernel<T><<<g, 256, 0, st>>>((int)nc, S, nc, Rr(0.5), Sa, nc);
+      MAK_CUDA_TRY(cudaGetLastError());
+    }
+    MAK_TRY(reduce_mat<T>(st, nc, nc, Sa, nc, 0, red, tmp));
+    note_launch();
+    sqrt_scalar_kernel<Rr><<<1, 1, 0, st>>>(tmp, gauge);
+    MAK_CUDA_TRY(cudaGetLastError());
+    if (gauge_atol >= 0) {
+      Rr g = (Rr)gauge_atol;
+      MAK_CUDA_TRY(cudaMemcpyAsync(gatol, &g, sizeof(Rr), cudaMemcpyHostToDevice, st));
+      MAK_CUDA_TRY(cudaStreamSynchronize(st));
+    } else {
+      MAK_TRY(reduce_mat<T>(st, m, nc, dN, lddn, 1, red, tmp));
+      note_launch();
+      eps34_kernel<Rr><<<1, 1, 0, st>>>(tmp, gatol);
+      MAK_CUDA_TRY(cudaGetLastError());
+    }
+    if (k > 0) {
+      // Q, R of A (positive gauge)
+      MAK_TRY(copy_mat<T>(st, m, n, A, lda, Ac, m));
+      {
+        Arena qa(tail, tail_bytes);
+        MAK_TRY(qr_run<T>(st, m, n, Ac, m, Qc, m, k, Rc, k, k, 1, 0, precision, qa, info));
+      }
+      // G1 = dN^H Q;  R^{-1};  X = G1 R^{-H};  dA -= N X
+      MAK_TRY(G(nc, k, m, one_<T>(), opnd<T>(dN, lddn, OP_C), opnd<T>(Qc, m), zero_<T>(), G1, nc));
+      {
+        Arena gj(tail, tail_bytes);
+        MAK_TRY(gje_inverse<T>(st, k, Rc, k, iperm, precision, gj, info));
+      }
+      note_launch();
+      gather_cols_kernel<T><<<dim3((unsigned)ceil_div(k, 128), (unsigned)k), 128, 0, st>>>(
+          (int)k, Rc, k, iperm, Rinv, k);
+      MAK_CUDA_TRY(cudaGetLastError());
+      MAK_TRY(G(nc, k, k, one_<T>(), opnd<T>(G1, nc), opnd<T>(Rinv, k, OP_C, MASK_UPPER),
+                zero_<T>(), X, nc));
+      MAK_TRY(G(m, k, nc, -one_<T>(), opnd<T>(N, ldn), opnd<T>(X, nc), one_<T>(), dA, ldda));
+    }
+  }
+  note_launch();
+  info_pullback_kernel<T><<<1, 1, 0, st>>>(info, (int)k, 0, gauge, gatol);
+  MAK_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// lq_pullback! (reference src/pullbacks/lq.jl:71-112) is the conjugate
+// transpose of qr_pullback! of A^H at (Q^H, L^H) with cotangents (dQ^H, dL^H):
+// the rank test, the gauge measures (max-abs norms) and every product of the
+// reference's LQ rule are the QR rule's, transposed.
+template <class T>
+static int lq_pullback_run(cudaStream_t st, int64_t m, int64_t n, int full, T* dA, int64_t ldda,
+                           const T* L, int64_t ldl, const T* Q, int64_t ldq, const T* dL,
+                           int64_t lddl, const T* dQ, int64_t lddq, double rank_atol,
+                           double gauge_atol, int precision, Arena& ar, mak_info* info) {
+  const int64_t k = m < n ? m : n;
+  const int64_t qr_ = (full && n > m) ? n : k;  // rows of Q, columns of L
+  const int64_t lq = qr_ > 0 ? qr_ : 1;
+  const int64_t ln = n > 0 ? n : 1;
+  T* Qt = ar.take<T>((size_t)n * qr_ + 1);
+  T* Rt = ar.take<T>((size_t)qr_ * m + 1);
+  T* dQt = dQ ? ar.take<T>((size_t)n * qr_ + 1) : nullptr;
+  T* dRt = dL ? ar.take<T>((size_t)qr_ * m + 1) : nullptr;
+  T* dB = ar.take<T>((size_t)n * m + 1);
+  size_t inner = 0;
+  {
+    Arena meas(nullptr, 0);
+    qr_pullback_run<T>(st, n, m, full, nullptr, ln, nullptr, ln, nullptr, lq, nullptr, ln,
+                       nullptr, lq, rank_atol, gauge_atol, precision, meas, nullptr);
+    inner = meas.off + 256;
+  }
+  char* sub = ar.take<char>(inner);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  MAK_TRY(ctranspose<T>(st, qr_, n, Q, ldq, Qt, ln));
+  MAK_TRY(ctranspose<T>(st, m, qr_, L, ldl, Rt, lq));
+  if (dQ) MAK_TRY(ctranspose<T>(st, qr_, n, dQ, lddq, dQt, ln));
+  if (dL) MAK_TRY(ctranspose<T>(st, m, qr_, dL, lddl, dRt, lq));
+  if (n * m > 0) MAK_CUDA_TRY(cudaMemsetAsync(dB, 0, (size_t)n * m * sizeof(T), st));
+  Arena a2(sub, inner);
+  MAK_TRY(qr_pullback_run<T>(st, n, m, full, dB, ln, Qt, ln, Rt, lq, dQt, ln, dRt, lq, rank_atol,
+                             gauge_atol, precision, a2, info));
+  return ctranspose<T>(st, n, m, dB, ln, dA, ldda, true);
+}
+
+// lq_null_pullback! (reference src/pullbacks/lq.jl:133-145): the conjugate
+// transpose of qr_null_pullback! of A^H at N = Nh^H with dN = dNh^H
+// (X = L^{-H} Q dNh^H, dA -= X Nh; the gauge ||antiherm(Nh dNh^H)||_F).
+template <class T>
+static int lq_null_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldda,
+                                const T* A, int64_t lda, const T* Nh, int64_t ldnh,
+                                const T* dNh, int64_t lddnh, double gauge_atol, int precision,
+                                Arena& ar, mak_info* info) {
+  const int64_t k = m < n ? m : n;
+  const int64_t nr = n - k;
+  const int64_t ln = n > 0 ? n : 1;
+  T* At = ar.take<T>((size_t)n * m + 1);
+  T* Nt = ar.take<T>((size_t)n * nr + 1);
+  T* dNt = ar.take<T>((size_t)n * nr + 1);
+  T* dB = ar.take<T>((size_t)n * m + 1);
+  size_t inner = 0;
+  {
+    Arena meas(nullptr, 0);
+    qr_null_pullback_run<T>(st, n, m, nullptr, ln, nullptr, ln, nullptr, ln, nullptr, ln,
+                            gauge_atol, precision, meas, nullptr);
+    inner = meas.off + 256;
+  }
+  char* sub = ar.take<char>(inner);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  MAK_TRY(ctranspose<T>(st, m, n, A, lda, At, ln));
+  MAK_TRY(ctranspose<T>(st, nr, n, Nh, ldnh, Nt, ln));
+  if (dNh) MAK_TRY(ctranspose<T>(st, nr, n, dNh, lddnh, dNt, ln));
+  if (n * m > 0) MAK_CUDA_TRY(cudaMemsetAsync(dB, 0, (size_t)n * m * sizeof(T), st));
+  Arena a2(sub, inner);
+  MAK_TRY(qr_null_pullback_run<T>(st, n, m, dB, ln, At, ln, Nt, ln, dNh ? dNt : nullptr, ln,
+                                  gauge_atol, precision, a2, info));
+  return ctranspose<T>(st, n, m, dB, ln, dA, ldda, true);
+}
+
+template <class T>
+static int qr_null_pullback_entry(int64_t m, int64_t n, void* dAv, int64_t ldda, const void* Av,
+                                  int64_t lda, const void* Nv, int64_t ldn, const void* dNv,
+                                  int64_t lddn, const mak_pullback_opts* opts, void* work,
+                                  size_t work_bytes, mak_info* info, mak_stream_t stream) {
+  const int64_t k = m < n ? m : n;
+  const int64_t nc = m - k;
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (dAv == nullptr && m * n > 0) return -3;
+  if (ldda < (m > 1 ? m : 1)) return -4;
+  if (Av == nullptr && m * n > 0) return -5;
+  if (lda < (m > 1 ? m : 1)) return -6;
+  if (Nv == nullptr && m * nc > 0) return -7;
+  if (ldn < (m > 1 ? m : 1)) return -8;
+  if (dNv && lddn < (m > 1 ? m : 1)) return -10;
+  mak_pullback_opts o{-1.0, -1.0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -11;
+  if (info == nullptr) return -14;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    qr_null_pullback_run<T>(st, m, n, nullptr, ldda, nullptr, lda, nullptr, ldn, nullptr, lddn,
+                            o.gauge_atol, o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -13;
+  }
+  MAK_TRY(info_reset(st, info));
+  Arena ar(work, work_bytes);
+  return qr_null_pullback_run<T>(st, m, n, (T*)dAv, ldda, (const T*)Av, lda, (const T*)Nv, ldn,
+                                 (const T*)dNv, lddn, o.gauge_atol, o.precision, ar, info);
+}
+
+template <class T>
+static int lq_pullback_entry(int64_t m, int64_t n, int full, void* dAv, int64_t ldda,
+                             const void* Lv, int64_t ldl, const void* Qv, int64_t ldq,
+                             const void* dLv, int64_t lddl, const void* dQv, int64_t lddq,
+                             const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                             mak_info* info, mak_stream_t stream) {
+  const int64_t k = m < n ? m : n;
+  const int64_t qr_ = (full && n > m) ? n : k;
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (dAv == nullptr && m * n > 0) return -4;
+  if (ldda < (m > 1 ? m : 1)) return -5;
+  if (Lv == nullptr && m * qr_ > 0) return -6;
+  if (ldl < (m > 1 ? m : 1)) return -7;
+  if (Qv == nullptr && qr_ * n > 0) return -8;
+  if (ldq < (qr_ > 1 ? qr_ : 1)) return -9;
+  if (dLv && lddl < (m > 1 ? m : 1)) return -11;
+  if (dQv && lddq < (qr_ > 1 ? qr_ : 1)) return -13;
+  mak_pullback_opts o{-1.0, -1.0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -14;
+  if (info == nullptr) return -17;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    lq_pullback_run<T>(st, m, n, full, nullptr, ldda, nullptr, ldl, nullptr, ldq,
+                       (const T*)dLv, lddl, (const T*)dQv, lddq, o.rank_atol, o.gauge_atol,
+                       o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -16;
+  }
+  MAK_TRY(info_reset(st, info));
+  Arena ar(work, work_bytes);
+  return lq_pullback_run<T>(st, m, n, full, (T*)dAv, ldda, (const T*)Lv, ldl, (const T*)Qv, ldq,
+                            (const T*)dLv, lddl, (const T*)dQv, lddq, o.rank_atol, o.gauge_atol,
+                            o.precision, ar, info);
+}
+
+template <class T>
+static int lq_null_pullback_entry(int64_t m, int64_t n, void* dAv, int64_t ldda, const void* Av,
+                                  int64_t lda, const void* Nhv, int64_t ldnh, const void* dNhv,
+                                  int64_t lddnh, const mak_pullback_opts* opts, void* work,
+                                  size_t work_bytes, mak_info* info, mak_stream_t stream) {
+  const int64_t k = m < n ? m : n;
+  const int64_t nr = n - k;
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (dAv == nullptr && m * n > 0) return -3;
+  if (ldda < (m > 1 ? m : 1)) return -4;
+  if (Av == nullptr && m * n > 0) return -5;
+  if (lda < (m > 1 ? m : 1)) return -6;
+  if (Nhv == nullptr && nr * n > 0) return -7;
+  if (ldnh < (nr > 1 ? nr : 1)) return -8;
+  if (dNhv && lddnh < (nr > 1 ? nr : 1)) return -10;
+  mak_pullback_opts o{-1.0, -1.0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (o.precision != MAK_PREC_NATIVE && o.precision != MAK_PREC_MIXED) return -11;
+  if (info == nullptr) return -14;
+  cudaStream_t st = (cudaStream_t)stream;
+  {
+    Arena meas(nullptr, 0);
+    lq_null_pullback_run<T>(st, m, n, nullptr, ldda, nullptr, lda, nullptr, ldnh, nullptr, lddnh,
+                            o.gauge_atol, o.precision, meas, nullptr);
+    if (meas.off > work_bytes) return -13;
+  }
+  MAK_TRY(info_reset(st, info));
+  Arena ar(work, work_bytes);
+  return lq_null_pullback_run<T>(st, m, n, (T*)dAv, ldda, (const T*)Av, lda, (const T*)Nhv, ldnh,
+                                 (const T*)dNhv, lddnh, o.gauge_atol, o.precision, ar, info);
+}
+
+template <class T>
+static size_t qr_null_pb_ws(int64_t m, int64_t n, int prec) {
+  Arena meas(nullptr, 0);
+  qr_null_pullback_run<T>(0, m, n, nullptr, m, nullptr, m, nullptr, m, nullptr, m, -1.0, prec,
+                          meas, nullptr);
+  return meas.off + 256;
+}
+template <class T>
+static size_t lq_pb_ws(int64_t m, int64_t n, int full, int prec) {
+  Arena meas(nullptr, 0);
+  T dummy;
+  // with both cotangents present (the larger workspace)
+  lq_pullback_run<T>(0, m, n, full, nullptr, m, nullptr, m, nullptr, n, &dummy, m, &dummy, n,
+                     -1.0, -1.0, prec, meas, nullptr);
+  return meas.off + 256;
+}
+template <class T>
+static size_t lq_null_pb_ws(int64_t m, int64_t n, int prec) {
+  Arena meas(nullptr, 0);
+  lq_null_pullback_run<T>(0, m, n, nullptr, m, nullptr, m, nullptr, n, nullptr, n, -1.0, prec,
+                          meas, nullptr);
+  return meas.off + 256;
+}
+
 template <class T>
 static size_t qr_pb_ws(int64_t m, int64_t n, int full, int prec) {
   Arena meas(nullptr, 0);
@@ -924,6 +1238,80 @@ MAK_RPOLPF(mak_right_polar_pushforward_d, double, double)
 MAK_RPOLPF(mak_right_polar_pushforward_z, zcomplex, void)
 MAK_RPOLPF(mak_right_polar_pushforward_s, float, float)
 MAK_RPOLPF(mak_right_polar_pushforward_c, ccomplex, void)
+
+int mak_qr_null_pullback_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                   size_t* bytes) {
+  if (bytes == nullptr) return -5;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  switch (dtype) {
+    case MAK_F64: *bytes = qr_null_pb_ws<double>(m, n, precision); break;
+    case MAK_C64: *bytes = qr_null_pb_ws<zcomplex>(m, n, precision); break;
+    case MAK_F32: *bytes = qr_null_pb_ws<float>(m, n, precision); break;
+    case MAK_C32: *bytes = qr_null_pb_ws<ccomplex>(m, n, precision); break;
+    default: return -1;
+  }
+  return 0;
+}
+
+int mak_lq_pullback_workspace(int dtype, int64_t m, int64_t n, int full, int precision,
+                              size_t* bytes) {
+  if (bytes == nullptr) return -6;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  switch (dtype) {
+    case MAK_F64: *bytes = lq_pb_ws<double>(m, n, full, precision); break;
+    case MAK_C64: *bytes = lq_pb_ws<zcomplex>(m, n, full, precision); break;
+    case MAK_F32: *bytes = lq_pb_ws<float>(m, n, full, precision); break;
+    case MAK_C32: *bytes = lq_pb_ws<ccomplex>(m, n, full, precision); break;
+    default: return -1;
+  }
+  return 0;
+}
+
+int mak_lq_null_pullback_workspace(int dtype, int64_t m, int64_t n, int precision,
+                                   size_t* bytes) {
+  if (bytes == nullptr) return -5;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  switch (dtype) {
+    case MAK_F64: *bytes = lq_null_pb_ws<double>(m, n, precision); break;
+    case MAK_C64: *bytes = lq_null_pb_ws<zcomplex>(m, n, precision); break;
+    case MAK_F32: *bytes = lq_null_pb_ws<float>(m, n, precision); break;
+    case MAK_C32: *bytes = lq_null_pb_ws<ccomplex>(m, n, precision); break;
+    default: return -1;
+  }
+  return 0;
+}
+
+#define MAK_NULLPB(NAME, FN, T, PT)                                                             \
+  int NAME(int64_t m, int64_t n, PT* dA, int64_t ldda, const PT* A, int64_t lda, const PT* N,   \
+           int64_t ldn, const PT* dN, int64_t lddn, const mak_pullback_opts* opts, void* work,  \
+           size_t work_bytes, mak_info* info, mak_stream_t stream) {                            \
+    return FN<T>(m, n, dA, ldda, A, lda, N, ldn, dN, lddn, opts, work, work_bytes, info,        \
+                 stream);                                                                       \
+  }
+MAK_NULLPB(mak_qr_null_pullback_d, qr_null_pullback_entry, double, double)
+MAK_NULLPB(mak_qr_null_pullback_z, qr_null_pullback_entry, zcomplex, void)
+MAK_NULLPB(mak_qr_null_pullback_s, qr_null_pullback_entry, float, float)
+MAK_NULLPB(mak_qr_null_pullback_c, qr_null_pullback_entry, ccomplex, void)
+MAK_NULLPB(mak_lq_null_pullback_d, lq_null_pullback_entry, double, double)
+MAK_NULLPB(mak_lq_null_pullback_z, lq_null_pullback_entry, zcomplex, void)
+MAK_NULLPB(mak_lq_null_pullback_s, lq_null_pullback_entry, float, float)
+MAK_NULLPB(mak_lq_null_pullback_c, lq_null_pullback_entry, ccomplex, void)
+
+#define MAK_LQPB(NAME, T, PT)                                                                   \
+  int NAME(int64_t m, int64_t n, int full, PT* dA, int64_t ldda, const PT* L, int64_t ldl,      \
+           const PT* Q, int64_t ldq, const PT* dL, int64_t lddl, const PT* dQ, int64_t lddq,    \
+           const mak_pullback_opts* opts, void* work, size_t work_bytes, mak_info* info,        \
+           mak_stream_t stream) {                                                               \
+    return lq_pullback_entry<T>(m, n, full, dA, ldda, L, ldl, Q, ldq, dL, lddl, dQ, lddq, opts, \
+                                work, work_bytes, info, stream);                                \
+  }
+MAK_LQPB(mak_lq_pullback_d, double, double)
+MAK_LQPB(mak_lq_pullback_z, zcomplex, void)
+MAK_LQPB(mak_lq_pullback_s, float, float)
+MAK_LQPB(mak_lq_pullback_c, ccomplex, void)
 
 #define MAK_POLPF(NAME, T, PT)                                                                  \
   int NAME(int64_t m, int64_t n, const PT* dA, int64_t ldda, const PT* W, int64_t ldw,          \

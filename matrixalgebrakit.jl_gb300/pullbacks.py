@@ -1,5 +1,6 @@
-"""Reverse rules: ``qr_pullback_``, ``left_polar_pullback_`` and
-``right_polar_pullback_`` on CUDA tensors.
+"""Reverse rules on CUDA tensors: ``qr_pullback_``, ``qr_null_pullback_``,
+``lq_pullback_``, ``lq_null_pullback_``, ``left_polar_pullback_`` and
+``right_polar_pullback_``.
 
 Mirror ``qr_pullback!(ΔA, A, (Q, R), (ΔQ, ΔR); rank_atol, gauge_atol)``
 (src/pullbacks/qr.jl:73-120) and ``left_polar_pullback!(ΔA, A, (W, P),
@@ -158,4 +159,101 @@ def right_polar_pullback_(dA, A, PWh, dPWh, precision="native", _info=None):
     check_status(inf, fn.__name__)
     if _info is not None:
         _info.update(iterations=inf.iterations)
+    return dA
+
+
+def _null_pullback(kind, dA, A, X, dX, gauge_atol, precision, _info):
+    """Shared driver of qr_null_pullback_ / lq_null_pullback_."""
+    check_cuda_tensor(dA, "dA")
+    check_cuda_tensor(A, "A")
+    m, n = A.shape
+    if tuple(dA.shape) != (m, n):
+        raise DimensionMismatch(f"dA must have size {(m, n)}")
+    k = min(m, n)
+    shape = (m, m - k) if kind == "qr_null" else (n - k, n)
+    _chk(A, (m, n), dA.dtype, "A")
+    _chk(X, shape, dA.dtype, "N" if kind == "qr_null" else "Nh")
+    _chk(dX, shape, dA.dtype, "dN" if kind == "qr_null" else "dNh")
+    opts = _opts(None, gauge_atol, precision)
+    L = lib()
+    nbytes = ct.c_size_t(0)
+    check_rc(getattr(L, f"mak_{kind}_pullback_workspace")(DTYPE_CODE[dA.dtype], m, n,
+                                                          opts.precision, ct.byref(nbytes)),
+             f"mak_{kind}_pullback_workspace")
+    dev = dA.device
+    ldx = ld_or_raise(X, "N") if X.numel() else max(1, shape[0])
+    with torch.cuda.device(dev):
+        work = workspace(nbytes.value, dev)
+        info = new_info(dev)
+        fn = getattr(L, f"mak_{kind}_pullback_{SUFFIX[dA.dtype]}")
+        rc = fn(m, n, ptr(dA), ld_or_raise(dA, "dA"), ptr(A), ld_or_raise(A, "A"),
+                ptr(X) if X.numel() else None, ldx, ptr(dX) if dX is not None else None,
+                ld_or_raise(dX, "dN") if dX is not None and dX.numel() else max(1, shape[0]),
+                ct.byref(opts), ptr(work), nbytes.value, ptr(info), stream_handle(dev))
+        check_rc(rc, fn.__name__)
+        inf = read_info(info)
+    check_status(inf, fn.__name__)
+    if inf.gauge > inf.gauge_atol:
+        warnings.warn(f"`{kind}` cotangent sensitive to gauge choice: (|Δgauge| = {inf.gauge})",
+                      RuntimeWarning, stacklevel=3)
+    if _info is not None:
+        _info.update(gauge=inf.gauge, gauge_atol=inf.gauge_atol)
+    return dA
+
+
+def qr_null_pullback_(dA, A, N, dN, gauge_atol=None, precision="native", _info=None):
+    """``qr_null_pullback!(ΔA, A, N, ΔN; gauge_atol)`` (src/pullbacks/qr.jl:141-152):
+    dA -= N (ΔN^H Q) R^{-H} with (Q, R) = qr_compact(A; positive = true)
+    recomputed on the device; warns on a gauge-dependent cotangent (qr.jl:122-128)."""
+    return _null_pullback("qr_null", dA, A, N, dN, gauge_atol, precision, _info)
+
+
+def lq_null_pullback_(dA, A, Nh, dNh, gauge_atol=None, precision="native", _info=None):
+    """``lq_null_pullback!(ΔA, A, Nᴴ, ΔNᴴ; gauge_atol)`` (src/pullbacks/lq.jl:133-145):
+    dA -= L^{-H} (Q ΔNᴴ^H) Nᴴ with (L, Q) = lq_compact(A; positive = true)."""
+    return _null_pullback("lq_null", dA, A, Nh, dNh, gauge_atol, precision, _info)
+
+
+def lq_pullback_(dA, A, LQ, dLQ, rank_atol=None, gauge_atol=None, precision="native",
+                 _info=None):
+    """``lq_pullback!(ΔA, A, (L, Q), (ΔL, ΔQ); rank_atol, gauge_atol)``
+    (src/pullbacks/lq.jl:71-112): dA += (pullback of lq_compact / lq_full at
+    (L, Q)), computed as the conjugate transpose of the QR rule on A^H."""
+    L_, Q = LQ
+    dL, dQ = dLQ
+    check_cuda_tensor(dA, "dA")
+    m, n = L_.shape[0], Q.shape[1]
+    if tuple(dA.shape) != (m, n):
+        raise DimensionMismatch(f"size of dA ({tuple(dA.shape)}) does not match size of L*Q "
+                                f"({m}, {n})")
+    full = int(n > m and Q.shape[0] == n)
+    k = min(m, n)
+    qr_ = n if full else k
+    _chk(L_, (m, qr_), dA.dtype, "L")
+    _chk(Q, (qr_, n), dA.dtype, "Q")
+    _chk(dL, L_.shape, dA.dtype, "dL")
+    _chk(dQ, Q.shape, dA.dtype, "dQ")
+    opts = _opts(rank_atol, gauge_atol, precision)
+    lb = lib()
+    nbytes = ct.c_size_t(0)
+    check_rc(lb.mak_lq_pullback_workspace(DTYPE_CODE[dA.dtype], m, n, full, opts.precision,
+                                          ct.byref(nbytes)), "mak_lq_pullback_workspace")
+    dev = dA.device
+    with torch.cuda.device(dev):
+        work = workspace(nbytes.value, dev)
+        info = new_info(dev)
+        fn = getattr(lb, f"mak_lq_pullback_{SUFFIX[dA.dtype]}")
+        rc = fn(m, n, full, ptr(dA), ld_or_raise(dA, "dA"), ptr(L_), ld_or_raise(L_, "L"),
+                ptr(Q), ld_or_raise(Q, "Q"), ptr(dL),
+                ld_or_raise(dL, "dL") if dL is not None else 1, ptr(dQ),
+                ld_or_raise(dQ, "dQ") if dQ is not None else 1, ct.byref(opts), ptr(work),
+                nbytes.value, ptr(info), stream_handle(dev))
+        check_rc(rc, fn.__name__)
+        inf = read_info(info)
+    check_status(inf, fn.__name__)
+    if inf.gauge > inf.gauge_atol:
+        warnings.warn(f"`lq` cotangents sensitive to gauge choice: (|Δgauge| = {inf.gauge})",
+                      RuntimeWarning, stacklevel=2)
+    if _info is not None:
+        _info.update(rank=inf.rank, gauge=inf.gauge, gauge_atol=inf.gauge_atol)
     return dA

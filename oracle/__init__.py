@@ -13,7 +13,14 @@ libblastrampoline), the reference's CPU algorithms:
 * ``PolarViaSVD``           -- src/implementations/polar.jl:59-95
 * ``PolarNewton``           -- src/implementations/polar.jl:99-166,209-220
 * ``qr_pullback!``          -- src/pullbacks/qr.jl:1-120
+* ``qr_null_pullback!``     -- src/pullbacks/qr.jl:122-152,198-200
 * ``left_polar_pullback!``  -- src/pullbacks/polar.jl:7-29
+* ``right_polar_pullback!`` -- src/pullbacks/polar.jl:37-59
+* polar pushforwards        -- src/pushforwards/polar.jl:1-26
+* LQ via the transposed QR  -- src/implementations/lq.jl:303-326, and the
+  Native row-Householder LQ (lq.jl:177-219) as its independent check
+* ``lq_pullback!``, ``lq_null_pullback!`` -- src/pullbacks/lq.jl:1-196
+* ``right_polar!(::PolarNewton)`` -- src/implementations/polar.jl:113-125,168-206
 
 Parity status: the reference ships no golden vectors for this path (its tests
 are property based, test/testsuite/decompositions/{qr,polar}.jl) and Julia is

@@ -24,7 +24,9 @@ __all__ = [
     "is_complex", "real_dtype", "eps",
     "lq_via_qr", "lq_compact", "lq_full", "lq_householder_native", "right_polar_newton",
     "right_polar_svd", "right_polar_pullback", "left_polar_pushforward",
-    "right_polar_pushforward",
+    "right_polar_pushforward", "qr_null_pullback", "remove_qr_null_gauge_dependence",
+    "lq_pullback", "remove_lq_gauge_dependence", "lq_null_pullback",
+    "remove_lq_null_gauge_dependence", "lq_null",
 ]
 
 
@@ -166,6 +168,12 @@ def lq_compact(A, positive: bool = True, blocksize: int = 0):
 def lq_full(A, positive: bool = True, blocksize: int = 0):
     """``lq_full!`` through the transposed QR (see ``lq_via_qr``)."""
     return lq_via_qr(A, full=True, positive=positive, blocksize=blocksize)
+
+
+def lq_null(A, positive: bool = True):
+    """``lq_null!`` through ``lq_null_via_qr!`` (src/implementations/lq.jl:
+    320-326): the conjugate transpose of ``qr_null`` of A^H."""
+    return np.asfortranarray(qr_null(np.asarray(A).conj().T, positive=positive).conj().T)
 
 
 def _householder_vec(v):
@@ -486,6 +494,150 @@ def remove_qr_gauge_dependence(dQ, dR, A, Q, R, rank_atol=None):
         d = np.arange(k - r)
         dR[r + d, r + d] = 0
     return dQ, dR
+
+
+def qr_null_pullback(dA, A, N, dN, gauge_atol=None):
+    """``qr_null_pullback!(dA, A, N, dN)`` (src/pullbacks/qr.jl:141-152) with
+    ``check_qr_null_cotangents`` (qr.jl:122-128).  Returns ``(dA, info)``."""
+    dA = np.array(dA, order="F", copy=True)
+    N = np.asarray(N)
+    info = {"dgauge": 0.0, "gauge_atol": 0.0, "warn": False}
+    if dN is None or N.shape[1] == 0:
+        return dA, info
+    dN = np.asarray(dN)
+    if gauge_atol is None:
+        gauge_atol = default_atol(dN)
+    S = N.conj().T @ dN
+    dgauge = float(np.linalg.norm((S - S.conj().T) / 2))
+    info = {"dgauge": dgauge, "gauge_atol": gauge_atol, "warn": dgauge > gauge_atol}
+    Q, R = qr_compact(A, positive=True)
+    # rdiv!(dN^H Q, UpperTriangular(R)') = (dN^H Q) R^{-H}
+    G = dN.conj().T @ Q
+    X = sla.solve_triangular(R, G.conj().T, trans="N", lower=False).conj().T \
+        if R.size else G
+    dA -= N @ X
+    return dA, info
+
+
+def remove_qr_null_gauge_dependence(dN, A, N):
+    """``remove_qr_null_gauge_dependence!`` (src/pullbacks/qr.jl:198-200):
+    dN - N (N^H dN)."""
+    N = np.asarray(N)
+    return np.asarray(dN) - N @ (N.conj().T @ np.asarray(dN))
+
+
+def lq_pullback(dA, A, L, Q, dL, dQ, rank_atol=None, gauge_atol=None):
+    """``lq_pullback!(dA, A, (L, Q), (dL, dQ))`` (src/pullbacks/lq.jl:71-112)
+    with ``check_and_prepare_lq_cotangents`` (lq.jl:3-55), restated directly on
+    the rows of Q (not through the transposed QR rule).  ``dL``/``dQ`` may be
+    ``None``.  Returns ``(dA, info)``."""
+    dA = np.array(dA, order="F", copy=True)
+    L = np.asarray(L)
+    Q = np.asarray(Q)
+    m, n = L.shape[0], Q.shape[1]
+    k = min(m, n)
+    if rank_atol is None:
+        rank_atol = default_atol(L)
+    if gauge_atol is None:
+        gauge_atol = default_atol(dQ) if dQ is not None else 0.0
+    p = qr_rank(L, rank_atol)  # lq_rank = qr_rank of L (the diagonal of L)
+    if dA.shape != (m, n):
+        raise ValueError("size of dA does not match size of L*Q")
+    L11 = np.tril(L[:p, :p])
+    L21 = L[p:m, :p]
+    Q1 = Q[:p, :]
+    dgauge = 0.0
+    dQ1 = np.zeros((p, n), dtype=Q.dtype)
+    if dQ is not None:
+        dQ = np.asarray(dQ)
+        dQ1[:] = dQ[:p, :n]
+        if p == k:
+            dQ3 = dQ[k:Q.shape[0], :].copy()
+            Q3 = Q[k:Q.shape[0], :]
+            dQ3Q1h = dQ3 @ Q1.conj().T
+            dQ3 = dQ3 - dQ3Q1h @ Q1
+            dgauge_q = float(np.max(np.abs(dQ3))) if dQ3.size else 0.0
+            dQ1 = dQ1 - dQ3Q1h.conj().T @ Q3
+        else:
+            dQ2 = dQ[p:Q.shape[0], :]
+            dgauge_q = float(np.max(np.abs(dQ2))) if dQ2.size else 0.0
+        dgauge = max(dgauge, dgauge_q)
+    if dL is not None:
+        dL = np.asarray(dL)
+        dL11 = np.tril(dL[:p, :p])
+        dL21 = dL[p:m, :p]
+        if p < k:
+            dL22 = dL[p:m, p:k]
+            dgauge = max(dgauge, float(np.max(np.abs(np.tril(dL22)))))
+    if dL is not None and m > p:
+        dQ1 = dQ1 - (L21.conj().T @ dL21) @ Q1
+        dA[p:m, :] += dL21 @ Q1
+    M = np.zeros((p, p), dtype=Q.dtype)
+    if dL is not None:
+        M += L11.conj().T @ dL11
+    M -= dQ1 @ Q1.conj().T
+    il = np.tril_indices(p, -1)
+    M[il[1], il[0]] = np.conj(M[il[0], il[1]])
+    if is_complex(M.dtype):
+        d = np.arange(p)
+        M[d, d] = M[d, d].real
+    dQ1 = dQ1 + M @ Q1
+    # ldiv!(L11', dQ1): L11^{-H} dQ1
+    if p:
+        dA[:p, :] += sla.solve_triangular(L11, dQ1, trans="C", lower=True)
+    return dA, {"rank": p, "dgauge": dgauge, "gauge_atol": gauge_atol,
+                "warn": bool(dgauge > gauge_atol)}
+
+
+def remove_lq_gauge_dependence(dL, dQ, A, L, Q, rank_atol=None):
+    """``remove_lq_gauge_dependence!`` (src/pullbacks/lq.jl:155-186)."""
+    dL = np.array(dL, copy=True)
+    dQ = np.array(dQ, copy=True)
+    m, n = np.shape(A)
+    k = min(m, n)
+    r = qr_rank(L, rank_atol)
+    Q1 = Q[:r, :]
+    dQ[r:k, :] = 0
+    if r == k and dQ.shape[0] > k:
+        dQ[k:, :] = (dQ[k:, :] @ Q1.conj().T) @ Q1
+    else:
+        dQ[k:, :] = 0
+    sub = dL[r:, r:k]
+    d = np.arange(min(sub.shape))
+    sub[d, d] = 0
+    if r < k:
+        sub[np.tril_indices(sub.shape[0], 0, sub.shape[1])] = 0
+    dL[r:, r:k] = sub
+    return dL, dQ
+
+
+def lq_null_pullback(dA, A, Nh, dNh, gauge_atol=None):
+    """``lq_null_pullback!(dA, A, Nh, dNh)`` (src/pullbacks/lq.jl:133-145) with
+    ``check_lq_null_cotangents`` (lq.jl:114-120).  Returns ``(dA, info)``."""
+    dA = np.array(dA, order="F", copy=True)
+    Nh = np.asarray(Nh)
+    info = {"dgauge": 0.0, "gauge_atol": 0.0, "warn": False}
+    if dNh is None or Nh.shape[0] == 0:
+        return dA, info
+    dNh = np.asarray(dNh)
+    if gauge_atol is None:
+        gauge_atol = default_atol(dNh)
+    S = Nh @ dNh.conj().T
+    dgauge = float(np.linalg.norm((S - S.conj().T) / 2))
+    info = {"dgauge": dgauge, "gauge_atol": gauge_atol, "warn": dgauge > gauge_atol}
+    L, Q = lq_compact(A, positive=True)
+    # ldiv!(LowerTriangular(L)', Q dNh^H) = L^{-H} (Q dNh^H)
+    G = Q @ dNh.conj().T
+    X = sla.solve_triangular(L, G, trans="C", lower=True) if L.size else G
+    dA -= X @ Nh
+    return dA, info
+
+
+def remove_lq_null_gauge_dependence(dNh, A, Nh):
+    """``remove_lq_null_gauge_dependence!`` (src/pullbacks/lq.jl:194-196):
+    dNh - (dNh Nh^H) Nh."""
+    Nh = np.asarray(Nh)
+    return np.asarray(dNh) - (np.asarray(dNh) @ Nh.conj().T) @ Nh
 
 
 def sylvester(A, B, C):

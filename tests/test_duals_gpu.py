@@ -281,3 +281,118 @@ def test_pushforward_mixed_precision(mak, cuda):
     dW, dP = mak.left_polar_pushforward_(to_dev(E, cuda), None,
                                          (to_dev(W, cuda), to_dev(P, cuda)), precision="mixed")
     assert O.rel_err(to_host(dW), dWo) <= 1e-9 and O.rel_err(to_host(dP), dPo) <= 1e-9
+
+
+# ------------------------------------------------- null-space and LQ pullbacks ---
+
+@pytest.mark.parametrize("dt", DTS, ids=lambda d: np.dtype(d).name)
+@pytest.mark.parametrize("shape", [(23, 9), (80, 30)])
+def test_qr_null_pullback_vs_oracle_and_fd(mak, cuda, dt, shape):
+    rng = np.random.default_rng(74)
+    A = O.gaussian(rng, *shape, dt)
+    N = O.qr_null(A)
+    dN = O.remove_qr_null_gauge_dependence(O.gaussian(rng, *N.shape, dt), A, N)
+    dA0 = O.gaussian(rng, *shape, dt)
+    ref, oinfo = O.qr_null_pullback(dA0, A, N, dN)
+    dA = to_dev(dA0, cuda)
+    info = {}
+    mak.qr_null_pullback_(dA, to_dev(A, cuda), to_dev(N, cuda), to_dev(dN, cuda), _info=info)
+    got = to_host(dA)
+    assert O.rel_err(got - dA0, ref - dA0) <= 1e-11
+    assert info["gauge"] <= info["gauge_atol"] and not oinfo["warn"]
+    E = O.gaussian(rng, *shape, dt)
+    h = 1e-6
+
+    def loss(X):
+        return float(np.real(np.vdot(dN, to_host(mak.qr_null(to_dev(X, cuda))))))
+
+    fd = (loss(A + h * E) - loss(A - h * E)) / (2 * h)
+    an = float(np.real(np.vdot(got - dA0, E)))
+    assert abs(fd - an) <= 1e-6 * max(1.0, abs(fd))
+
+
+def test_qr_null_pullback_gauge_warning_and_empty(mak, cuda):
+    rng = np.random.default_rng(75)
+    A = O.gaussian(rng, 30, 10, np.complex128)
+    N = O.qr_null(A)
+    dN = N @ (1j * np.eye(20))  # N^H dN = i I: purely gauge
+    dA = to_dev(np.zeros_like(A), cuda)
+    with pytest.warns(RuntimeWarning, match="gauge"):
+        mak.qr_null_pullback_(dA, to_dev(A, cuda), to_dev(N, cuda), to_dev(dN, cuda))
+    # square A: the null space is empty and nothing is added
+    B = O.gaussian(rng, 12, 12, np.float64)
+    dB0 = O.gaussian(rng, 12, 12, np.float64)
+    dB = to_dev(dB0, cuda)
+    Ne = torch.empty((12, 0), dtype=torch.float64, device=cuda)
+    mak.qr_null_pullback_(dB, to_dev(B, cuda), Ne, Ne)
+    assert np.array_equal(to_host(dB), dB0)
+
+
+@pytest.mark.parametrize("dt", DTS, ids=lambda d: np.dtype(d).name)
+def test_lq_null_pullback_vs_oracle_and_fd(mak, cuda, dt):
+    rng = np.random.default_rng(76)
+    A = O.gaussian(rng, 9, 23, dt)
+    Nh = O.lq_null(A)
+    dNh = O.remove_lq_null_gauge_dependence(O.gaussian(rng, *Nh.shape, dt), A, Nh)
+    ref, _ = O.lq_null_pullback(np.zeros_like(A), A, Nh, dNh)
+    dA = to_dev(np.zeros_like(A), cuda)
+    mak.lq_null_pullback_(dA, to_dev(A, cuda), to_dev(Nh, cuda), to_dev(dNh, cuda))
+    got = to_host(dA)
+    assert O.rel_err(got, ref) <= 1e-11
+    E = O.gaussian(rng, 9, 23, dt)
+    h = 1e-6
+
+    def loss(X):
+        return float(np.real(np.vdot(dNh, to_host(mak.lq_null(to_dev(X, cuda))))))
+
+    fd = (loss(A + h * E) - loss(A - h * E)) / (2 * h)
+    assert abs(fd - float(np.real(np.vdot(got, E)))) <= 1e-6 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("dt", DTS, ids=lambda d: np.dtype(d).name)
+@pytest.mark.parametrize("shape", [(17, 19), (19, 19), (19, 17), (50, 120)])
+def test_lq_pullback_vs_oracle_and_fd(mak, cuda, dt, shape):
+    rng = np.random.default_rng(77)
+    A = O.gaussian(rng, *shape, dt)
+    E = O.gaussian(rng, *shape, dt)
+    for full in (False, True):
+        f = O.lq_full if full else O.lq_compact
+        L, Q = f(A)
+        dL, dQ = O.gaussian(rng, *L.shape, dt), O.gaussian(rng, *Q.shape, dt)
+        dL, dQ = O.remove_lq_gauge_dependence(dL, dQ, A, L, Q)
+        dA0 = O.gaussian(rng, *shape, dt)
+        ref, oinfo = O.lq_pullback(dA0, A, L, Q, dL, dQ)
+        dA = to_dev(dA0, cuda)
+        info = {}
+        mak.lq_pullback_(dA, to_dev(A, cuda), (to_dev(L, cuda), to_dev(Q, cuda)),
+                         (to_dev(dL, cuda), to_dev(dQ, cuda)), _info=info)
+        got = to_host(dA)
+        assert info["rank"] == oinfo["rank"] == min(shape)
+        assert O.rel_err(got - dA0, ref - dA0) <= 1e-11
+        g = mak.lq_full if full else mak.lq_compact
+        h = 1e-6
+
+        def loss(X):
+            Lx, Qx = g(to_dev(X, cuda))
+            return float(np.real(np.vdot(dL, to_host(Lx)) + np.vdot(dQ, to_host(Qx))))
+
+        fd = (loss(A + h * E) - loss(A - h * E)) / (2 * h)
+        an = float(np.real(np.vdot(got - dA0, E)))
+        assert abs(fd - an) <= 1e-6 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("dt", DTS, ids=lambda d: np.dtype(d).name)
+def test_lq_pullback_rank_deficient_and_zero_tangents(mak, cuda, dt):
+    rng = np.random.default_rng(78)
+    A = O.rank_deficient(rng, 40, 60, 25, dt)
+    L, Q = O.lq_compact(A)
+    dL, dQ = O.gaussian(rng, *L.shape, dt), O.gaussian(rng, *Q.shape, dt)
+    dL, dQ = O.remove_lq_gauge_dependence(dL, dQ, A, L, Q)
+    for cot in ((dL, dQ), (None, dQ), (dL, None)):
+        ref, oinfo = O.lq_pullback(np.zeros_like(A), A, L, Q, *cot)
+        dA = to_dev(np.zeros_like(A), cuda)
+        info = {}
+        mak.lq_pullback_(dA, None, (to_dev(L, cuda), to_dev(Q, cuda)),
+                         tuple(None if c is None else to_dev(c, cuda) for c in cot), _info=info)
+        assert info["rank"] == oinfo["rank"] == 25
+        assert O.rel_err(to_host(dA), ref) <= 1e-9

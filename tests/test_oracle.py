@@ -277,3 +277,86 @@ def test_oracle_polar_pushforward_fd(dt):
     assert O.rel_err(dWh, fWh) < 1e-7 and O.rel_err(dPb, fPb) < 1e-7
     # conjugate-transpose duality: right pushforward of A^H = (left pushforward of A)^H
     assert O.rel_err(dWh, dW.conj().T) < 1e-12 and O.rel_err(dPb, dP.conj().T) < 1e-12
+
+
+# ------------------------------------------------- null-space and LQ pullbacks ---
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_qr_null_pullback_fd(dt):
+    """FD of Re<dN, qr_null(A)> with a gauge-invariant cotangent
+    (remove_qr_null_gauge_dependence!, src/pullbacks/qr.jl:198-200)."""
+    rng = np.random.default_rng(16)
+    A = O.gaussian(rng, 23, 9, dt)
+    N = O.qr_null(A)
+    dN = O.remove_qr_null_gauge_dependence(O.gaussian(rng, *N.shape, dt), A, N)
+    dA, info = O.qr_null_pullback(np.zeros_like(A), A, N, dN)
+    assert not info["warn"]
+    E = O.gaussian(rng, 23, 9, dt)
+    fd = _fd(lambda X: np.real(np.vdot(dN, O.qr_null(X))), A, E)
+    assert abs(fd - np.real(np.vdot(dA, E))) < 1e-7 * max(1, abs(fd))
+    # a gauge-dependent cotangent trips the check
+    _, info2 = O.qr_null_pullback(np.zeros_like(A), A, N, N @ (1j * np.eye(N.shape[1]) if
+                                  O.is_complex(dt) else np.triu(np.ones((14, 14)), 1)))
+    assert info2["warn"]
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_lq_null_pullback_fd(dt):
+    rng = np.random.default_rng(17)
+    A = O.gaussian(rng, 9, 23, dt)
+    Nh = O.lq_null(A)
+    assert Nh.shape == (14, 23) and np.linalg.norm(A @ Nh.conj().T) < 1e-12
+    dNh = O.remove_lq_null_gauge_dependence(O.gaussian(rng, *Nh.shape, dt), A, Nh)
+    dA, info = O.lq_null_pullback(np.zeros_like(A), A, Nh, dNh)
+    assert not info["warn"]
+    E = O.gaussian(rng, 9, 23, dt)
+    fd = _fd(lambda X: np.real(np.vdot(dNh, O.lq_null(X))), A, E)
+    assert abs(fd - np.real(np.vdot(dA, E))) < 1e-7 * max(1, abs(fd))
+    # conjugate-transpose duality with the QR null-space rule
+    dAt, _ = O.qr_null_pullback(np.zeros_like(A.T), A.conj().T, Nh.conj().T, dNh.conj().T)
+    assert O.rel_err(dAt.conj().T, dA) < 1e-12
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+@pytest.mark.parametrize("shape", [(17, 19), (19, 19), (19, 17)])
+def test_oracle_lq_pullback_fd(dt, shape):
+    """test/testsuite/chainrules.jl pattern for lq_compact and lq_full."""
+    rng = np.random.default_rng(18)
+    A = O.gaussian(rng, *shape, dt)
+    E = O.gaussian(rng, *shape, dt)
+    for full in (False, True):
+        f = O.lq_full if full else O.lq_compact
+        L, Q = f(A)
+        dL, dQ = O.gaussian(rng, *L.shape, dt), O.gaussian(rng, *Q.shape, dt)
+        dL, dQ = O.remove_lq_gauge_dependence(dL, dQ, A, L, Q)
+        dA, info = O.lq_pullback(np.zeros_like(A), A, L, Q, dL, dQ)
+        assert not info["warn"] and info["rank"] == min(shape)
+
+        def loss(X):
+            Lx, Qx = f(X)
+            return np.real(np.vdot(dL, Lx) + np.vdot(dQ, Qx))
+
+        fd = _fd(loss, A, E)
+        assert abs(fd - np.real(np.vdot(dA, E))) < 1e-7 * max(1, abs(fd))
+        dAt, _ = O.qr_pullback(np.zeros_like(A.T), A.conj().T, Q.conj().T, L.conj().T,
+                               dQ.conj().T, dL.conj().T)
+        assert O.rel_err(dAt.conj().T, dA) < 1e-12
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_oracle_lq_pullback_rank_deficient_fd(dt):
+    rng = np.random.default_rng(19)
+    A = O.rank_deficient(rng, 20, 30, 14, dt)
+    L, Q = O.lq_compact(A)
+    dL, dQ = O.gaussian(rng, *L.shape, dt), O.gaussian(rng, *Q.shape, dt)
+    dL, dQ = O.remove_lq_gauge_dependence(dL, dQ, A, L, Q)
+    dA, info = O.lq_pullback(np.zeros_like(A), A, L, Q, dL, dQ)
+    assert info["rank"] == 14 and not info["warn"]
+    E = A @ np.linalg.pinv(A) @ O.gaussian(rng, 20, 30, dt) @ np.linalg.pinv(A) @ A
+
+    def loss(X):
+        Lx, Qx = O.lq_compact(X)
+        return np.real(np.vdot(dL, Lx) + np.vdot(dQ, Qx))
+
+    fd = _fd(loss, A, E)
+    assert abs(fd - np.real(np.vdot(dA, E))) < 1e-6 * max(1, abs(fd))
