@@ -52,3 +52,14 @@ __all__ += ["qr_pullback_", "left_polar_pullback_", "right_polar_pullback_", "qr
 from .batched import batched_left_polar, batched_qr_compact  # noqa: E402
 
 __all__ += ["batched_qr_compact", "batched_left_polar"]
+
+from .algorithms import RightOrthViaLQ, RightOrthViaPolar  # noqa: E402
+from .orthnull import (batched_left_orth, batched_project_isometric, left_null,  # noqa: E402
+                       left_null_, left_orth, left_orth_, left_orth_alg, project_isometric,
+                       project_isometric_, right_null, right_null_, right_orth, right_orth_,
+                       right_orth_alg)
+
+__all__ += ["RightOrthViaLQ", "RightOrthViaPolar", "left_orth", "left_orth_", "right_orth",
+            "right_orth_", "left_null", "left_null_", "right_null", "right_null_",
+            "project_isometric", "project_isometric_", "left_orth_alg", "right_orth_alg",
+            "batched_left_orth", "batched_project_isometric"]

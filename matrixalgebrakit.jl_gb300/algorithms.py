@@ -96,6 +96,21 @@ class LeftOrthViaPolar:
     alg: GB300_PolarNewton = field(default_factory=GB300_PolarNewton)
 
 
+@dataclass(frozen=True)
+class RightOrthViaLQ:
+    """``right_orth`` through an LQ algorithm (src/interface/orthnull.jl,
+    implementations/orthnull.jl:91)."""
+
+    alg: LQViaTransposedQR = field(default_factory=LQViaTransposedQR)
+
+
+@dataclass(frozen=True)
+class RightOrthViaPolar:
+    """``right_orth`` through a (right) polar algorithm (orthnull.jl:92)."""
+
+    alg: GB300_PolarNewton = field(default_factory=GB300_PolarNewton)
+
+
 ALGORITHMS = {c.__name__: c for c in (GB300_HouseholderQR, GB300_PolarNewton)}
 
 _QR_FUNCS = ("qr_compact", "qr_compact_", "qr_full", "qr_full_", "qr_null", "qr_null_")

@@ -159,3 +159,24 @@ def test_dual_algorithm_selection(mak):
     assert isinstance(alg, LQViaTransposedQR) and alg.alg.blocksize == 8
     assert select_algorithm("lq_compact", None, None, positive=False).positive is False
     assert select_algorithm("qr_compact_", None, GB300_HouseholderQR()) == GB300_HouseholderQR()
+
+
+def test_orth_algorithm_selection(mak):
+    """src/interface/orthnull.jl:414-456: kind symbols and algorithm instances."""
+    from mak_gb300 import (ArgumentError, GB300_HouseholderQR, GB300_PolarNewton, LeftOrthViaPolar,
+                           LeftOrthViaQR, LQViaTransposedQR, RightOrthViaLQ, RightOrthViaPolar,
+                           left_orth_alg, right_orth_alg)
+
+    assert left_orth_alg() == LeftOrthViaQR(GB300_HouseholderQR())
+    assert left_orth_alg("polar", maxiter=7) == LeftOrthViaPolar(GB300_PolarNewton(maxiter=7))
+    assert left_orth_alg(GB300_PolarNewton()) == LeftOrthViaPolar(GB300_PolarNewton())
+    assert right_orth_alg() == RightOrthViaLQ(LQViaTransposedQR(GB300_HouseholderQR()))
+    assert right_orth_alg(GB300_HouseholderQR(blocksize=4)).alg.alg.blocksize == 4
+    assert right_orth_alg("polar") == RightOrthViaPolar(GB300_PolarNewton())
+    for bad in ("svd", "nope"):
+        with pytest.raises(ArgumentError):
+            left_orth_alg(bad)
+        with pytest.raises(ArgumentError):
+            right_orth_alg(bad)
+    with pytest.raises(ArgumentError):
+        left_orth_alg(GB300_HouseholderQR(), positive=False)
