@@ -4,7 +4,23 @@
 #include "gemm.cuh"
 #include "internal.h"
 
+#include <cstdlib>
+#include <mutex>
+
 namespace mak {
+
+double split_min_mnk() {
+  static double v = 67108864.0;  // 2^26
+  static std::once_flag f;
+  std::call_once(f, [] {
+    const char* e = getenv("MAK_SPLIT_MIN_MNK");
+    if (e && *e) {
+      const double x = atof(e);
+      if (x >= 1.0 && x <= 1e15) v = x;
+    }
+  });
+  return v;
+}
 
 // C = alpha * sum_s part[s] + beta * C  (fixed summation order)
 template <class T>
@@ -29,7 +45,7 @@ static int gemm_native(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha
     // measuring: a bound valid for every smaller output too (pick_splits
     // keeps splits * tiles <= 4 * SMs), since the split count grows as the
     // output shrinks while call sites measure at their largest shape
-    if (K > 256) {
+    if (K > 64) {  // pick_splits keeps >= 64 of K per split
       const size_t bound = (size_t)4 * num_sms() * 64 * 64;
       const size_t cap = (size_t)64 * (size_t)(M > 0 ? M : 1) * (size_t)(N > 0 ? N : 1);
       ar.take<T>(bound < cap ? bound : cap);
@@ -70,7 +86,7 @@ int gemm_prec(cudaStream_t st, int precision, int64_t M, int64_t N, int64_t K, T
         return 0;
       }
       const double work = (traits<T>::cpx ? 4.0 : 1.0) * (double)M * (double)N * (double)K;
-      if (precision == PREC_SPLIT_ALWAYS || work >= SPLIT_MIN_MNK)
+      if (precision == PREC_SPLIT_ALWAYS || work >= split_min_mnk())
         return oz_gemm<T>(st, M, N, K, alpha, A, B, beta, C, ldc, ar, status, max_ctas);
     }
   }

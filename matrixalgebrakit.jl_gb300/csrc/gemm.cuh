@@ -175,7 +175,7 @@ inline int pick_splits(int64_t M, int64_t N, int64_t K, int sms) {
   int64_t want = 2LL * sms;
   if (tiles >= want) return 1;
   int64_t s = ceil_div(want, tiles);
-  int64_t maxs = ceil_div(K, 256);  // keep >= 256 of K per split
+  int64_t maxs = ceil_div(K, 64);  // keep >= 64 of K per split
   if (s > maxs) s = maxs;
   if (s < 1) s = 1;
   if (s > 64) s = 64;

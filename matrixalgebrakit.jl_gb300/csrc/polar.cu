@@ -239,7 +239,7 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
   // elimination runs even when mixed precision is asked for
   const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8 &&
                      (traits<T>::cpx ? 4.0 : 1.0) * (double)n * (double)n * GJ_OUTER_NB >=
-                         8.0 * SPLIT_MIN_MNK;
+                         8.0 * split_min_mnk();
   const int NBO = mixed ? GJ_OUTER_NB : GJ_NB;
   int* piv = ar.take<int>(n > 0 ? n : 1);
   real_t<T>* part_val = ar.take<real_t<T>>(sms);

@@ -647,7 +647,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   // problems run the native blocking even when mixed precision is asked for
   const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8 &&
                      (traits<T>::cpx ? 4.0 : 1.0) * (double)m * (double)n * QR_OUTER_NB >=
-                         SPLIT_MIN_MNK;
+                         split_min_mnk();
   const int NBO = mixed ? QR_OUTER_NB : nb;
   const int64_t nblk_o = ceil_div(k, NBO);
 
