@@ -43,7 +43,9 @@ struct GjArgs {
   int* piv;
   real_t<T>* part_val;
   int* part_idx;
-  T* swapbuf;  // [2][GJ_NB]
+  T* swapbuf;  // [2][GJ_NB]: row jj by column parity
+  T* cand;     // [2][gstride][GJ_NB]: each CTA's pivot candidate row, by column parity
+  int gstride;  // allocation stride of the per-CTA partials
   unsigned* bar;
   int* status;
   int* singular;
@@ -64,12 +66,13 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
   using R = real_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x b, ld = rpc
+  T* fsh = Ps + (size_t)a.rpc * a.b;        // rpc multipliers of the current column
   __shared__ R sv[32];
   __shared__ int si[32];
   __shared__ T prow[GJ_NB];
   __shared__ T srow[GJ_NB];
   __shared__ T dinv_s;
-  __shared__ int pivs;
+  __shared__ int pivs, pivq;
   const int G = gridDim.x, cb = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
   const int rpc = a.rpc, b = a.b, k0 = a.k0;
@@ -80,9 +83,22 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
     for (int r = tid; r < nr; r += blockDim.x) Ps[r + c * rpc] = Xp[(r0 + r) + (int64_t)c * a.ldx];
   __syncthreads();
 
+  // Per column one grid-wide round: every CTA publishes its local arg-max
+  // (value desc, index asc) together with that candidate row, and the CTA
+  // holding row jj publishes row jj.  After the barrier every CTA merges the
+  // partials in the same fixed order, reads the winning candidate as the
+  // pivot row, and the CTA holding the pivot's old row receives row jj: no
+  // second round for the exchange.  The published values are
+  // double-buffered by column parity (a CTA writes column j+1's slot only
+  // after every CTA passed barrier j, i.e. finished reading column j-1's).
   for (int j = 0; j < b; j++) {
     const int jj = k0 + j;
-    // ---- pivot search over global rows >= jj
+    const int par = j & 1;
+    R* pval = a.part_val + par * a.gstride;
+    int* pidx = a.part_idx + par * a.gstride;
+    T* rowjj = a.swapbuf + par * GJ_NB;
+    T* cand = a.cand + (int64_t)par * a.gstride * GJ_NB;
+    // ---- local pivot candidate over global rows >= jj
     R best = R(-1);
     int bidx = INT_MAX;
     for (int r = tid; r < nr; r += blockDim.x) {
@@ -96,40 +112,62 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
       amax_merge(best, bidx, v2, i2);
     }
     if (lane == 0) { sv[wid] = best; si[wid] = bidx; }
+    if (jj >= r0 && jj < r0 + nr)
+      for (int c = tid; c < b; c += blockDim.x) rowjj[c] = Ps[(jj - r0) + c * rpc];
     __syncthreads();
-    if (tid == 0) {
-      for (int w = 1; w < nw; w++) amax_merge(best, bidx, sv[w], si[w]);
-      a.part_val[cb] = best;
-      a.part_idx[cb] = bidx;
-    }
-    if (!grid_barrier(a.bar, G, a.status)) return;
-
-    // ---- global pivot (identical in every CTA), publish the two rows
     if (wid == 0) {
-      R v = R(-1);
-      int ix = INT_MAX;
-      for (int q = lane; q < G; q += 32) amax_merge(v, ix, ld_cg(&a.part_val[q]), ld_cg(&a.part_idx[q]));
+      R v = lane < nw ? sv[lane] : R(-1);
+      int ix = lane < nw ? si[lane] : INT_MAX;
 #pragma unroll
       for (int m = 16; m > 0; m >>= 1) {
         R v2 = __shfl_xor_sync(0xffffffffu, v, m);
         int i2 = __shfl_xor_sync(0xffffffffu, ix, m);
         amax_merge(v, ix, v2, i2);
       }
-      if (lane == 0) pivs = (ix == INT_MAX) ? jj : ix;
+      if (lane == 0) {
+        pval[cb] = v;
+        pidx[cb] = ix;
+        pivs = ix;
+      }
     }
     __syncthreads();
-    const int p = pivs;
-    if (jj >= r0 && jj < r0 + nr)
-      for (int c = tid; c < b; c += blockDim.x) a.swapbuf[c] = Ps[(jj - r0) + c * rpc];
-    if (p >= r0 && p < r0 + nr)
-      for (int c = tid; c < b; c += blockDim.x) a.swapbuf[GJ_NB + c] = Ps[(p - r0) + c * rpc];
-    if (cb == 0 && tid == 0) a.piv[jj] = p;
+    {
+      const int li = pivs;  // this CTA's candidate row (global index)
+      if (li != INT_MAX)
+        for (int c = tid; c < b; c += blockDim.x)
+          cand[(int64_t)cb * GJ_NB + c] = Ps[(li - r0) + c * rpc];
+    }
     if (!grid_barrier(a.bar, G, a.status)) return;
 
-    // ---- exchange rows jj <-> p, then eliminate column jj from every other row
-    for (int c = tid; c < b; c += blockDim.x) prow[c] = ld_cg(&a.swapbuf[GJ_NB + c]);
+    // ---- global pivot (identical in every CTA), then the exchange
+    if (wid == 0) {
+      R v = R(-1);
+      int ix = INT_MAX, iq = -1;
+      for (int q = lane; q < G; q += 32) {
+        const R v2 = ld_cg(&pval[q]);
+        const int i2 = ld_cg(&pidx[q]);
+        if (v2 > v || (v2 == v && i2 < ix)) { v = v2; ix = i2; iq = q; }
+      }
+#pragma unroll
+      for (int m = 16; m > 0; m >>= 1) {
+        R v2 = __shfl_xor_sync(0xffffffffu, v, m);
+        int i2 = __shfl_xor_sync(0xffffffffu, ix, m);
+        int q2 = __shfl_xor_sync(0xffffffffu, iq, m);
+        if (v2 > v || (v2 == v && i2 < ix)) { v = v2; ix = i2; iq = q2; }
+      }
+      if (lane == 0) {
+        pivs = (ix == INT_MAX) ? jj : ix;
+        pivq = (ix == INT_MAX || ix == jj) ? -1 : iq;
+      }
+    }
+    __syncthreads();
+    const int p = pivs, q = pivq;
+    // pivot row: the winning CTA's candidate (row jj itself when p == jj)
+    for (int c = tid; c < b; c += blockDim.x)
+      prow[c] = q < 0 ? ld_cg(&rowjj[c]) : ld_cg(&cand[(int64_t)q * GJ_NB + c]);
     if (p != jj && p >= r0 && p < r0 + nr)
-      for (int c = tid; c < b; c += blockDim.x) Ps[(p - r0) + c * rpc] = ld_cg(&a.swapbuf[c]);
+      for (int c = tid; c < b; c += blockDim.x) Ps[(p - r0) + c * rpc] = ld_cg(&rowjj[c]);
+    if (cb == 0 && tid == 0) a.piv[jj] = p;
     __syncthreads();
     if (tid == 0) {
       const T d = prow[j];
@@ -143,16 +181,18 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
     // element); its own column holds the new pivot-column entry 1/d
     for (int c = tid; c < b; c += blockDim.x) srow[c] = (c == j) ? dinv : prow[c] * dinv;
     __syncthreads();
-    for (int r = tid; r < nr; r += blockDim.x) {
-      const int gr = r0 + r;
-      if (gr == jj) {
-        for (int c = 0; c < b; c++) Ps[r + c * rpc] = srow[c];
-      } else {
-        const T f = Ps[r + j * rpc];
-        for (int c = 0; c < b; c++) {
-          if (c == j) Ps[r + c * rpc] = -(f * dinv);
-          else Ps[r + c * rpc] = fma_(-f, srow[c], Ps[r + c * rpc]);
-        }
+    // the rows' multipliers f_r = X[r, jj] first, then the elimination with
+    // each warp on its own columns (lanes over rows), so that all eight
+    // warps share the FP64 work even when a CTA owns only a few dozen rows
+    for (int r = tid; r < nr; r += blockDim.x) fsh[r] = Ps[r + j * rpc];
+    __syncthreads();
+    for (int c = wid; c < b; c += nw) {
+      const T sc = srow[c];
+      T* pc = Ps + c * rpc;
+      for (int r = lane; r < nr; r += 32) {
+        if (r0 + r == jj) pc[r] = sc;
+        else if (c == j) pc[r] = -(fsh[r] * dinv);
+        else pc[r] = fma_(-fsh[r], sc, pc[r]);
       }
     }
     __syncthreads();
@@ -242,9 +282,11 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
                          8.0 * split_min_mnk();
   const int NBO = mixed ? GJ_OUTER_NB : GJ_NB;
   int* piv = ar.take<int>(n > 0 ? n : 1);
-  real_t<T>* part_val = ar.take<real_t<T>>(sms);
-  int* part_idx = ar.take<int>(sms);
+  // per-CTA pivot partials and candidate rows, double-buffered by column parity
+  real_t<T>* part_val = ar.take<real_t<T>>(2 * sms);
+  int* part_idx = ar.take<int>(2 * sms);
   T* swapbuf = ar.take<T>(2 * GJ_NB);
+  T* cand = ar.take<T>((size_t)2 * sms * GJ_NB);
   T* buf = ar.take<T>((size_t)NBO * (n > 0 ? n : 1));
   T* bufo = mixed ? ar.take<T>((size_t)NBO * (n > 0 ? n : 1)) : nullptr;
   unsigned* bar = ar.take<unsigned>(2);
@@ -273,21 +315,22 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
     // grid: rows per CTA >= 64, at most one CTA per SM, slab within shared memory
     int64_t G = ceil_div(n, 64);
     if (G > max_ctas) G = max_ctas;
+    // the slab holds rpc x (b + 1) values: the panel rows and their multipliers
     int64_t rpc = ceil_div(n, G);
-    if ((size_t)rpc * b * sizeof(T) > cap) {
-      G = ceil_div(n, (int64_t)(cap / ((size_t)b * sizeof(T))));
+    if ((size_t)rpc * (b + 1) * sizeof(T) > cap) {
+      G = ceil_div(n, (int64_t)(cap / ((size_t)(b + 1) * sizeof(T))));
       if (G > sms) return MAK_ERR_UNSUPPORTED;
       rpc = ceil_div(n, G);
     }
     G = ceil_div(n, rpc);
-    size_t smem = (size_t)rpc * b * sizeof(T);
+    size_t smem = (size_t)rpc * (b + 1) * sizeof(T);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_kernel<T>, GJ_THREADS,
                                                       smem) != cudaSuccess ||
         (int64_t)per_sm * sms < G)
       return MAK_ERR_UNSUPPORTED;
     GjArgs<T> ga{X, ldx, (int)n, (int)k0, b, (int)rpc, piv, part_val, part_idx, swapbuf,
-                 bar, &info->status, &info->singular};
+                 cand, sms, bar, &info->status, &info->singular};
     void* args[] = {&ga};
     ProfScope prof(s, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
     note_launch();

@@ -11,13 +11,15 @@
 // Structure on the device, per panel of jb <= 32 columns starting at j0:
 //  1. qr_panel_kernel: ONE cooperative launch factors the (m-j0) x jb panel.
 //     Each CTA keeps a contiguous slab of panel rows resident in shared
-//     memory for the whole panel; a column costs two bounded grid barriers
-//     (reflector norm, then the w = v^H A row vector).  Norms are plain sums
-//     of squares with a rescaled second pass when the largest magnitude is
+//     memory for the whole panel; a column costs one bounded grid barrier:
+//     the reflector norm and the dot products of the still unscaled column
+//     with the columns to its right are published together, and w = v^H A
+//     follows from them once beta/tau are known.  Norms are plain sums of
+//     squares with a rescaled two-round path when the largest magnitude is
 //     outside a safe range, and every cross-CTA reduction is done in a fixed
-//     order, so all CTAs derive bit-identical beta/tau.  The panel's
-//     Gram matrix V^H V is reduced at the end and CTA 0 forms the T factor
-//     (forward, column-wise larft recurrence).
+//     order, so all CTAs derive bit-identical beta/tau/w.  The panel's Gram
+//     matrix V^H V is reduced at the end and the CTAs form the T factor's
+//     columns (forward, column-wise larft recurrence).
 //  2. larfb on the trailing columns:  W = V^H C (split-K GEMM, V read in
 //     place through a unit-lower mask), W2 = T^H W (reduce_trmm_kernel),
 //     C -= V W2 (GEMM).
@@ -46,10 +48,12 @@ struct PanelArgs {
   int rpc;              // panel rows owned by one CTA
   T* tau;               // [jb]
   T* Tm;                // [NBMAX x NBMAX], ld NBMAX
-  real_t<T>* part_nrm;  // [3][gstride]: sums of squares, largest magnitudes, rescaled sums
-  T* part_w;            // [G][NBMAX]: w partials, one row of NBMAX columns per CTA
+  real_t<T>* part_nrm;  // [2][3][gstride] by column parity (sums of squares, largest
+                        // magnitudes, spare), then [gstride] rescaled sums
+  T* part_w;            // [2][gstride][NBMAX] dot partials by column parity, then
+                        // [gstride][NBMAX] for the rescaled path
   T* part_g;            // [G][NBMAX*NBMAX]
-  T* alpha_buf;         // [NBMAX]
+  T* alpha_buf;         // [2][NBMAX]: row j of the panel by column parity
   T* gram;              // [NBMAX*NBMAX]: the panel's reduced Gram matrix V^H V
   unsigned* bar;        // grid barrier words
   int* status;
@@ -119,7 +123,7 @@ template <class R> __device__ __forceinline__ int norm_needs_rescale(typename No
 // square root; values are scaled by exact powers of two, and magnitudes near
 // the ends of the exponent range take the IEEE operations.
 template <class T>
-__device__ void larfg_scalars(T alpha, real_t<T> xnorm, T& beta, T& tau, T& scal) {
+__device__ __forceinline__ void larfg_scalars(T alpha, real_t<T> xnorm, T& beta, T& tau, T& scal) {
   using R = real_t<T>;
   R ar = re_(alpha), ai = im_(alpha);
   if (xnorm == R(0) && ai == R(0)) {
@@ -157,11 +161,46 @@ __device__ void larfg_scalars(T alpha, real_t<T> xnorm, T& beta, T& tau, T& scal
   }
 }
 
+// The same scalars from the sum of squares ssq = |x|^2 and the largest
+// component magnitude amax of x, without forming |x| first: |beta| =
+// sqrt(|alpha|^2 + ssq) is one square root, which saves a whole Newton
+// chain on the column's critical path.  Scaling by w = max(|alpha|, amax)
+// (a power of two) keeps the scaled sum within [1, 2 (n + 1)].
 template <class T>
-__global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a) {
+__device__ __forceinline__ void larfg_scalars_ssq(T alpha, real_t<T> ssq, real_t<T> amax, T& beta, T& tau,
+                                  T& scal) {
+  using R = real_t<T>;
+  const R ar = re_(alpha), ai = im_(alpha);
+  const R w = fmax(fmax(fabs(ar), fabs(ai)), amax);
+  const int ew = exp2_of(w);
+  const int lim = sizeof(R) == 8 ? 1000 : 100;
+  if (ssq == R(0) || !(w > R(0)) || ew < -lim + 4 || ew > lim - 4) {
+    larfg_scalars(alpha, sqrt_nr_safe(ssq), beta, tau, scal);
+    return;
+  }
+  const R sd = pow2_(R(0), -ew), su = pow2_(R(0), ew);  // exact scalings
+  const R a1 = ar * sd, a2 = ai * sd;
+  const R s3 = (ssq * sd) * sd;
+  const R nrm = sqrt_nr(fma_(a1, a1, fma_(a2, a2, s3))) * su;
+  const R b = ar >= R(0) ? -nrm : nrm;
+  const R rb = rcp_nr(b);
+  beta = make_scalar<T>(b, 0);
+  tau = make_scalar<T>((b - ar) * rb, -ai * rb);
+  const R zr = ar - b;
+  if constexpr (traits<T>::cpx) {
+    const R z1 = zr * sd, z2 = ai * sd;
+    const R d = rcp_nr(fma_(z1, z1, z2 * z2)) * sd;
+    scal = make_scalar<T>(z1 * d, -z2 * d);
+  } else {
+    scal = make_scalar<T>(rcp_nr(zr), 0);
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T> a) {
   using R = real_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x jb, column-major, ld = rpc
+  T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x jb, column-major, ld = ldp
   __shared__ R red_r[32];
   __shared__ typename NormKey<R>::K red_k[32];
   __shared__ R sc_r[3];
@@ -169,60 +208,97 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
   __shared__ T wsh[NBMAX];
   __shared__ T red_w[PANEL_THREADS / 32][NBMAX];
   __shared__ T sc[3];
+  __shared__ T rowj[NBMAX];
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
   const int rpc = a.rpc, jb = a.jb;
+  const int ldp = rpc | 1;  // slab leading dimension (odd: conflict-free column strides)
   const int r0 = b * rpc;
   const int nr = max(0, min(a.mp, r0 + rpc) - r0);
 
   for (int c = 0; c < jb; c++)
-    for (int r = tid; r < nr; r += blockDim.x) Ps[r + c * rpc] = a.A[(r0 + r) + (int64_t)c * a.lda];
+    for (int r = tid; r < nr; r += blockDim.x) Ps[r + c * ldp] = a.A[(r0 + r) + (int64_t)c * a.lda];
   __syncthreads();
 
+  // Per column one grid-wide reduction: the partial sums of squares of x =
+  // column j below the diagonal, its largest magnitude, the partial dot
+  // products d_c = sum_{r>j} conj(x_r) A[r, c] of the still unscaled x with
+  // the columns c > j, and row j, all published in one round.  Since
+  // v = [1; scal x], w_c = v^H A[:, c] = A[j, c] + conj(scal) d_c follows
+  // once larfg has fixed scal, without a second round.  The partials are
+  // double-buffered by column parity: a CTA writes column j+1's slot only
+  // after every CTA passed barrier j, i.e. finished reading column j-1's.
+  // A column whose largest magnitude lies outside [2^lo, 2^hi] takes the
+  // rescaled two-round path instead (the same decision in every CTA).
   for (int j = 0; j < jb; j++) {
-    T* col = Ps + j * rpc;
-    // ---- phase A: partial sum of squares and largest magnitude of x =
-    // column j below the diagonal
+    T* col = Ps + j * ldp;
+    const int par = j & 1;
+    R* pn = a.part_nrm + (int64_t)par * 3 * a.gstride;
+    T* pw = a.part_w + (int64_t)par * a.gstride * NBMAX;
+    T* prow = a.alpha_buf + par * NBMAX;
     using NK = NormKey<R>;
     using Key = typename NK::K;
-    const int rs = max(0, j + 1 - r0);
-    R ssq = R(0);
-    Key mk = 0;
-    for (int r = rs + tid; r < nr; r += blockDim.x) {
-      const T x = col[r];
-      ssq = sq_add(ssq, x);
-      const Key k = mag_key(x);
-      mk = k > mk ? k : mk;
-    }
-    ssq = warp_sum(ssq);
-    mk = warp_max_key(mk);
-    __syncthreads();
-    if (lane == 0) {
-      red_r[wid] = ssq;
-      red_k[wid] = mk;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      R s = R(0);
-      Key m = 0;
-      for (int w = 0; w < nw; w++) {
-        s += red_r[w];
-        m = red_k[w] > m ? red_k[w] : m;
+    const int rs = max(0, j + 1 - r0);  // first local row below the diagonal
+    // ---- phase A: warp w takes a slice of this CTA's rows below the
+    // diagonal; lane c >= j accumulates conj(x_r) A[r, c] over the slice
+    // (lane j: conj(x_r) x_r, the sum of squares) and the largest magnitude
+    // of x.  No cross-lane reductions (GB300 issues about two FP64
+    // operations per clock per SM, so butterflies over 32 lanes would cost
+    // more than the products); warp 0 adds the eight slices.  The slab's
+    // odd leading dimension keeps the column-strided reads conflict-free.
+    {
+      const int nx = nr - rs;
+      const int per = nx > 0 ? (nx + nw - 1) / nw : 0;
+      const int ra = rs + wid * per, rb = min(nr, ra + per);
+      T s0 = zero_<T>(), s1 = zero_<T>();
+      Key mk = 0;
+      if (lane >= j && lane < jb) {
+        const T* pc = Ps + lane * ldp;
+        int r = ra;
+        for (; r + 1 < rb; r += 2) {
+          const T x0 = col[r], x1 = col[r + 1];
+          s0 = fma_(conj_(x0), pc[r], s0);
+          s1 = fma_(conj_(x1), pc[r + 1], s1);
+          const Key k0 = mag_key(x0), k1 = mag_key(x1);
+          const Key k = k0 > k1 ? k0 : k1;
+          mk = k > mk ? k : mk;
+        }
+        if (r < rb) {
+          const T x0 = col[r];
+          s0 = fma_(conj_(x0), pc[r], s0);
+          const Key k = mag_key(x0);
+          mk = k > mk ? k : mk;
+        }
       }
-      a.part_nrm[b] = s;
-      a.part_nrm[a.gstride + b] = NK::val(m);
-      if (j >= r0 && j < r0 + nr) a.alpha_buf[j] = col[j - r0];
+      red_w[wid][lane] = s0 + s1;
+      if (lane == j) red_k[wid] = mk;
+    }
+    if (j >= r0 && j < r0 + nr)
+      for (int c = j + tid; c < jb; c += blockDim.x) prow[c] = Ps[(j - r0) + c * ldp];
+    __syncthreads();
+    if (wid == 0) {
+      T s = zero_<T>();
+      for (int w = 0; w < nw; w++) s += red_w[w][lane];
+      if (lane > j && lane < jb) pw[(int64_t)b * NBMAX + lane] = s;
+      if (lane == j) {
+        Key m = 0;
+        for (int w = 0; w < nw; w++) m = red_k[w] > m ? red_k[w] : m;
+        pn[b] = re_(s);
+        pn[a.gstride + b] = NK::val(m);
+      }
     }
     if (!grid_barrier(a.bar, G, a.status)) return;
 
     // ---- phase B: every CTA combines the partials in the same fixed order
-    // and so derives bit-identical beta / tau
+    // and so derives bit-identical beta / tau / w.  Warp 0: the norm; every
+    // warp: a slice of the CTAs' dot partials (lane = column); lane j of
+    // warp 1 (or of warp 0 with one warp): row j.
     if (wid == 0) {
       R s = R(0);
       Key m = 0;
       for (int q = lane; q < G; q += 32) {
-        s += ld_cg(&a.part_nrm[q]);
-        const Key k = NK::key(ld_cg(&a.part_nrm[a.gstride + q]));
+        s += ld_cg(&pn[q]);
+        const Key k = NK::key(ld_cg(&pn[a.gstride + q]));
         m = k > m ? k : m;
       }
       s = warp_sum(s);
@@ -233,9 +309,27 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
         sc_flag = norm_needs_rescale<R>(m);
       }
     }
+    {
+      const int per = (G + nw - 1) / nw;
+      const int q0 = wid * per, q1 = min(G, q0 + per);
+      T a0 = zero_<T>(), a1 = zero_<T>(), a2 = zero_<T>(), a3 = zero_<T>();
+      if (lane > j && lane < jb) {
+        int q = q0;
+        for (; q + 3 < q1; q += 4) {
+          a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
+          a1 += ld_cg(&pw[(int64_t)(q + 1) * NBMAX + lane]);
+          a2 += ld_cg(&pw[(int64_t)(q + 2) * NBMAX + lane]);
+          a3 += ld_cg(&pw[(int64_t)(q + 3) * NBMAX + lane]);
+        }
+        for (; q < q1; q++) a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
+      }
+      red_w[wid][lane] = (a0 + a1) + (a2 + a3);
+    }
+    if (wid == (nw > 1 ? 1 : 0) && lane >= j && lane < jb) rowj[lane] = ld_cg(&prow[lane]);
     __syncthreads();
+    const bool rescale = sc_flag != 0;
     R xnorm = R(0);  // meaningful in thread 0 only (the scalars below)
-    if (sc_flag) {
+    if (rescale) {
       // rare: rescale by 2^-e, e the exponent of the largest magnitude
       // (clamped so the scale itself stays finite), then sum again
       int e = 0;
@@ -245,11 +339,11 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
       R ss2 = R(0);
       for (int r = rs + tid; r < nr; r += blockDim.x) ssq_scaled_add(ss2, col[r], scale);
       ss2 = block_sum(ss2, red_r);
-      if (tid == 0) a.part_nrm[2 * a.gstride + b] = ss2;
+      if (tid == 0) a.part_nrm[6 * a.gstride + b] = ss2;
       if (!grid_barrier(a.bar, G, a.status)) return;
       if (wid == 0) {
         R s2 = R(0);
-        for (int q = lane; q < G; q += 32) s2 += ld_cg(&a.part_nrm[2 * a.gstride + q]);
+        for (int q = lane; q < G; q += 32) s2 += ld_cg(&a.part_nrm[6 * a.gstride + q]);
         s2 = warp_sum(s2);
         if (lane == 0) sc_r[2] = sqrt(s2) * ldexp(R(1), e);
       }
@@ -257,10 +351,9 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
       xnorm = sc_r[2];
     }
     if (tid == 0) {
-      if (!sc_flag) xnorm = sqrt_nr_safe(sc_r[0]);
-      T alpha = ld_cg(&a.alpha_buf[j]);
       T beta, tau, scal;
-      larfg_scalars(alpha, xnorm, beta, tau, scal);
+      if (rescale) larfg_scalars(rowj[j], xnorm, beta, tau, scal);
+      else larfg_scalars_ssq(rowj[j], sc_r[0], sc_r[1], beta, tau, scal);
       sc[0] = beta;
       sc[1] = tau;
       sc[2] = scal;
@@ -268,51 +361,69 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
     __syncthreads();
     const T beta = sc[0], tau = sc[1], scal = sc[2];
     if (b == 0 && tid == 0) a.tau[j] = tau;
-    for (int r = rs + tid; r < nr; r += blockDim.x) col[r] = col[r] * scal;
-    if (tid == 0 && j >= r0 && j < r0 + nr) col[j - r0] = beta;
+    if (j + 1 >= jb) {
+      for (int r = rs + tid; r < nr; r += blockDim.x) col[r] = col[r] * scal;
+      if (tid == 0 && j >= r0 && j < r0 + nr) col[j - r0] = beta;
+      __syncthreads();
+      break;
+    }
+    if (!rescale) {
+      // f_c = conj(tau) w_c, w_c = A[j, c] + conj(scal) d_c, formed once
+      if (wid == 0) {
+        T sum = zero_<T>();
+        for (int w = 0; w < nw; w++) sum += red_w[w][lane];
+        if (lane > j && lane < jb) wsh[lane] = conj_(tau) * fma_(conj_(scal), sum, rowj[lane]);
+      }
+    } else {
+      // the two-round form on the scaled column: w = v^H A from v itself
+      for (int r = rs + tid; r < nr; r += blockDim.x) col[r] = col[r] * scal;
+      __syncthreads();
+      const int rj = max(0, j - r0);
+      T* pw2 = a.part_w + (int64_t)2 * a.gstride * NBMAX;
+      for (int c = j + 1 + wid; c < jb; c += nw) {
+        T s = zero_<T>();
+        for (int r = rj + lane; r < nr; r += 32) {
+          const T v = (r0 + r == j) ? one_<T>() : col[r];
+          s = fma_(conj_(v), Ps[r + c * ldp], s);
+        }
+        s = warp_sum(s);
+        if (lane == 0) pw2[(int64_t)b * NBMAX + c] = s;
+      }
+      if (!grid_barrier(a.bar, G, a.status)) return;
+      {
+        const int per = (G + nw - 1) / nw;
+        const int q0 = wid * per, q1 = min(G, q0 + per);
+        T acc = zero_<T>();
+        if (lane > j && lane < jb)
+          for (int q = q0; q < q1; q++) acc += ld_cg(&pw2[(int64_t)q * NBMAX + lane]);
+        red_w[wid][lane] = acc;
+      }
+      __syncthreads();
+      if (wid == 0) {
+        T sum = zero_<T>();
+        for (int w = 0; w < nw; w++) sum += red_w[w][lane];
+        if (lane > j && lane < jb) wsh[lane] = conj_(tau) * sum;
+      }
+    }
     __syncthreads();
-    if (j + 1 >= jb) break;
-
-    // partial w_c = sum_{r >= j} conj(v_r) A[r, c], c > j  (v_j = 1)
+    // ---- update rows >= j of the columns c > j: A[r, c] -= v_r f_c, with
+    // v_j = 1 and v_r = scal x_r below (stored back as the reflector)
+    // The reflector is scaled in place first; the update then gives each
+    // warp its own columns (lanes over rows), so that all eight warps share
+    // the FP64 work even when a CTA owns only a few dozen rows.
     const int rj = max(0, j - r0);
+    if (!rescale)
+      for (int r = rs + tid; r < nr; r += blockDim.x) col[r] = col[r] * scal;
+    __syncthreads();
     for (int c = j + 1 + wid; c < jb; c += nw) {
-      T s = zero_<T>();
-      for (int r = rj + lane; r < nr; r += 32) {
-        T v = (r0 + r == j) ? one_<T>() : col[r];
-        s = fma_(conj_(v), Ps[r + c * rpc], s);
-      }
-      s = warp_sum(s);
-      if (lane == 0) a.part_w[(int64_t)b * NBMAX + c] = s;
-    }
-    if (!grid_barrier(a.bar, G, a.status)) return;
-
-    // ---- phase C: combine w in a fixed order: lane = column, warp w sums
-    // the partials of a slice of the CTAs (coalesced rows of part_w), then
-    // warp 0 adds the slices; every CTA gets bit-identical w
-    {
-      const int per = (G + nw - 1) / nw;
-      const int q0 = wid * per, q1 = min(G, q0 + per);
-      T acc = zero_<T>();
-      if (lane > j && lane < jb)
-        for (int q = q0; q < q1; q++) acc += ld_cg(&a.part_w[(int64_t)q * NBMAX + lane]);
-      red_w[wid][lane] = acc;
-    }
-    __syncthreads();
-    if (wid == 0) {
-      T sum = zero_<T>();
-      for (int w = 0; w < nw; w++) sum += red_w[w][lane];
-      // the update's coefficient f_c = conj(tau) w_c, formed once per column
-      if (lane > j && lane < jb) wsh[lane] = conj_(tau) * sum;
-    }
-    __syncthreads();
-    for (int c = j + 1; c < jb; c++) {
       const T f = wsh[c];
-      T* pc = Ps + c * rpc;
-      for (int r = rj + tid; r < nr; r += blockDim.x) {
-        T v = (r0 + r == j) ? one_<T>() : col[r];
-        pc[r] -= v * f;
+      T* pc = Ps + c * ldp;
+      for (int r = rj + lane; r < nr; r += 32) {
+        const T v = (r0 + r == j) ? one_<T>() : col[r];
+        pc[r] = fma_(-v, f, pc[r]);
       }
     }
+    if (tid == 0 && j >= r0 && j < r0 + nr) col[j - r0] = beta;
     __syncthreads();
   }
 
@@ -328,18 +439,18 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
     const int rb = max(0, jj - r0);
     int r = rb;
     if (r < nr && r0 + r == jj) {  // v_jj = 1 on its diagonal row
-      s0 = conj_(Ps[r + i * rpc]);
+      s0 = conj_(Ps[r + i * ldp]);
       r++;
     }
     for (; r + 1 < nr; r += 2) {
-      s0 = fma_(conj_(Ps[r + i * rpc]), Ps[r + jj * rpc], s0);
-      s1 = fma_(conj_(Ps[r + 1 + i * rpc]), Ps[r + 1 + jj * rpc], s1);
+      s0 = fma_(conj_(Ps[r + i * ldp]), Ps[r + jj * ldp], s0);
+      s1 = fma_(conj_(Ps[r + 1 + i * ldp]), Ps[r + 1 + jj * ldp], s1);
     }
-    if (r < nr) s0 = fma_(conj_(Ps[r + i * rpc]), Ps[r + jj * rpc], s0);
+    if (r < nr) s0 = fma_(conj_(Ps[r + i * ldp]), Ps[r + jj * ldp], s0);
     a.part_g[(int64_t)b * NBMAX * NBMAX + i + jj * NBMAX] = s0 + s1;
   }
   for (int c = 0; c < jb; c++)
-    for (int r = tid; r < nr; r += blockDim.x) a.A[(r0 + r) + (int64_t)c * a.lda] = Ps[r + c * rpc];
+    for (int r = tid; r < nr; r += blockDim.x) a.A[(r0 + r) + (int64_t)c * a.lda] = Ps[r + c * ldp];
   if (!grid_barrier(a.bar, G, a.status)) return;
 
   // ---- reduce the Gram over the CTAs: one warp per pair, lanes over the
@@ -360,17 +471,28 @@ __global__ void __launch_bounds__(PANEL_THREADS) qr_panel_kernel(PanelArgs<T> a)
   // 1/tau_i and U_il = G_il (i < l), each column an independent back
   // substitution x_k = tau_k, x_i = -tau_i sum_{l=i+1..k} G_il x_l (tau_i as
   // a factor: tau_i = 0 needs no division).  Warp 0 of CTA c computes
-  // columns c, c + G, ...; lane i owns row i.
+  // columns c, c + G, ...; lane i owns row i.  tau and the strict upper
+  // triangle of the Gram matrix are staged in shared memory first (one
+  // batch of independent loads), so the substitution chain itself waits on
+  // no L2 round trip.
   if (wid != 0) return;
+  __shared__ T gs[NBMAX * NBMAX];
+  __shared__ T ts[NBMAX];
+  if (b < jb) {
+    for (int l = 1; l < jb; l++)
+      if (lane < l) gs[lane + l * NBMAX] = ld_cg(&a.gram[lane + l * NBMAX]);
+    ts[lane] = lane < jb ? ld_cg(&a.tau[lane]) : zero_<T>();
+  }
+  __syncwarp();
   for (int k = b; k < NBMAX; k += G) {
     T x = zero_<T>();
     if (k < jb) {
       T acc = zero_<T>();
       for (int l = k; l >= 0; l--) {
-        const T mine = (l == k) ? ld_cg(&a.tau[k]) : -(ld_cg(&a.tau[l]) * acc);
+        const T mine = (l == k) ? ts[k] : -(ts[l] * acc);
         const T xl = shfl_idx_(mine, l);
         if (lane == l) x = xl;
-        if (lane < l) acc = fma_(ld_cg(&a.gram[lane + l * NBMAX]), xl, acc);
+        if (lane < l) acc = fma_(gs[lane + l * NBMAX], xl, acc);
       }
     }
     a.Tm[lane + k * NBMAX] = (k < jb && lane <= k) ? x : zero_<T>();
@@ -604,7 +726,7 @@ template <class T>
 static int panel_shape(int64_t mp, int jb, PanelShape& ps, int want_ctas) {
   const int max_ctas = num_sms();
   const size_t cap = panel_slab_cap<T>();
-  int64_t rpc_max = (int64_t)(cap / ((size_t)jb * sizeof(T)));
+  int64_t rpc_max = (int64_t)(cap / ((size_t)jb * sizeof(T))) - 1;  // ld = rpc | 1
   int64_t G = ceil_div(mp, 64);
   if (G > want_ctas) G = want_ctas;
   if (G > max_ctas) G = max_ctas;
@@ -620,7 +742,7 @@ static int panel_shape(int64_t mp, int jb, PanelShape& ps, int want_ctas) {
   if (G < 1) G = 1;
   ps.G = (int)G;
   ps.rpc = (int)rpc;
-  ps.smem = (size_t)ps.rpc * jb * sizeof(T);
+  ps.smem = (size_t)(ps.rpc | 1) * jb * sizeof(T);
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_panel_kernel<T>, PANEL_THREADS,
                                                     ps.smem) != cudaSuccess)
@@ -656,10 +778,12 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   T* sgn = ar.take<T>(k > 0 ? k : 1);
   T* Wpart = ar.take<T>((size_t)max_splits * nb * (wmax > 0 ? wmax : 1));
   T* W2 = ar.take<T>((size_t)nb * (wmax > 0 ? wmax : 1));
-  real_t<T>* part_nrm = ar.take<real_t<T>>((size_t)3 * gmax);
-  T* part_w = ar.take<T>((size_t)gmax * NBMAX);
+  // norm partials [2 column parities][3][gmax] + the rescaled sums [gmax];
+  // dot partials [2 parities][gmax][NBMAX] + the rescaled path's [gmax][NBMAX]
+  real_t<T>* part_nrm = ar.take<real_t<T>>((size_t)7 * gmax);
+  T* part_w = ar.take<T>((size_t)3 * gmax * NBMAX);
   T* part_g = ar.take<T>((size_t)gmax * NBMAX * NBMAX);
-  T* alpha_buf = ar.take<T>(NBMAX);
+  T* alpha_buf = ar.take<T>(2 * NBMAX);  // row j of the panel, by column parity
   T* gram_buf = ar.take<T>((size_t)NBMAX * NBMAX);
   unsigned* bar = ar.take<unsigned>(2);
   T *To = nullptr, *Gm = nullptr, *Wm = nullptr, *W2m = nullptr;
