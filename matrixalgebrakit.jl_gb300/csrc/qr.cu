@@ -453,38 +453,49 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
     for (int r = tid; r < nr; r += blockDim.x) a.A[(r0 + r) + (int64_t)c * a.lda] = Ps[r + c * ldp];
   if (!grid_barrier(a.bar, G, a.status)) return;
 
-  // ---- reduce the Gram over the CTAs: one warp per pair, lanes over the
-  // CTAs' partials, fixed order
-  for (int pq = b * nw + wid; pq < npairs; pq += G * nw) {
+  // ---- reduce the Gram over the CTAs: one thread per pair, the CTAs'
+  // partials in a fixed order (four interleaved accumulators)
+  for (int pq = b * (int)blockDim.x + tid; pq < npairs; pq += G * (int)blockDim.x) {
     int jj = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)pq)) * 0.5f);
     while (jj * (jj - 1) / 2 > pq) jj--;
     while (jj * (jj + 1) / 2 <= pq) jj++;
     const int i = pq - jj * (jj - 1) / 2;
-    T s = zero_<T>();
-    for (int q = lane; q < G; q += 32) s += ld_cg(&a.part_g[(int64_t)q * NBMAX * NBMAX + i + jj * NBMAX]);
-    s = warp_sum(s);
-    if (lane == 0) a.gram[i + jj * NBMAX] = s;
+    const T* src = a.part_g + i + jj * NBMAX;
+    constexpr int64_t NN = NBMAX * NBMAX;
+    T s0 = zero_<T>(), s1 = zero_<T>(), s2 = zero_<T>(), s3 = zero_<T>();
+    int q = 0;
+    for (; q + 3 < G; q += 4) {
+      s0 += ld_cg(src + q * NN);
+      s1 += ld_cg(src + (q + 1) * NN);
+      s2 += ld_cg(src + (q + 2) * NN);
+      s3 += ld_cg(src + (q + 3) * NN);
+    }
+    for (; q < G; q++) s0 += ld_cg(src + q * NN);
+    a.gram[i + jj * NBMAX] = (s0 + s1) + (s2 + s3);
   }
   if (!grid_barrier(a.bar, G, a.status)) return;
 
   // ---- T factor (larft, forward, column-wise): T = U^{-1} with U_ii =
   // 1/tau_i and U_il = G_il (i < l), each column an independent back
   // substitution x_k = tau_k, x_i = -tau_i sum_{l=i+1..k} G_il x_l (tau_i as
-  // a factor: tau_i = 0 needs no division).  Warp 0 of CTA c computes
-  // columns c, c + G, ...; lane i owns row i.  tau and the strict upper
-  // triangle of the Gram matrix are staged in shared memory first (one
-  // batch of independent loads), so the substitution chain itself waits on
-  // no L2 round trip.
-  if (wid != 0) return;
+  // a factor: tau_i = 0 needs no division).  Column k goes to warp k mod 8
+  // of CTA k / 8 (then every G * 8 columns); lane i owns row i.  tau and the
+  // strict upper triangle of the Gram matrix are staged in shared memory
+  // first (one batch of independent loads), so the substitution chain
+  // itself waits on no L2 round trip.
+  const int kfirst = b * nw;
+  if (kfirst >= NBMAX) return;  // the same for every thread of the CTA
   __shared__ T gs[NBMAX * NBMAX];
   __shared__ T ts[NBMAX];
-  if (b < jb) {
-    for (int l = 1; l < jb; l++)
-      if (lane < l) gs[lane + l * NBMAX] = ld_cg(&a.gram[lane + l * NBMAX]);
-    ts[lane] = lane < jb ? ld_cg(&a.tau[lane]) : zero_<T>();
+  if (kfirst < jb) {
+    for (int e = tid; e < NBMAX * NBMAX; e += blockDim.x) {
+      const int i = e % NBMAX, l = e / NBMAX;
+      if (i < l && l < jb) gs[e] = ld_cg(&a.gram[e]);
+    }
+    if (tid < NBMAX) ts[tid] = tid < jb ? ld_cg(&a.tau[tid]) : zero_<T>();
   }
-  __syncwarp();
-  for (int k = b; k < NBMAX; k += G) {
+  __syncthreads();
+  for (int k = kfirst + wid; k < NBMAX; k += G * nw) {
     T x = zero_<T>();
     if (k < jb) {
       T acc = zero_<T>();
