@@ -86,8 +86,9 @@ def parse():
     ap.add_argument("--no-pullback", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-tensors", type=int, default=256)
-    ap.add_argument("--workload", choices=["qr", "gemm"], default="qr",
-                    help="gemm: time the split-precision product alone on --gemm-shapes")
+    ap.add_argument("--workload", choices=["qr", "gemm", "polar"], default="qr",
+                    help="gemm: time the split-precision product alone on --gemm-shapes; "
+                         "polar: left_polar! alone on --polar-n (profiling runs)")
     ap.add_argument("--gemm-shapes", type=str, default="16384x8192x128,128x8192x16384",
                     help="MxNxK list for --workload gemm (the trailing-update shapes of the "
                          "16384 x 8192 QR: C -= V W2 and W = V^H C)")
@@ -803,12 +804,29 @@ def run_gemm(args):
     return 0
 
 
+def run_polar_only(args):
+    """left_polar! alone (one warm-up and one timed factorization of the
+    --polar-n test matrix) in the requested precision: the small case the
+    Gauss-Jordan panel profiles are captured on."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    mak = ge.load_package()
+    print(json.dumps(polar_measure(mak, args, dev, args.precision)), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "gemm":
         return run_gemm(args)
+    if args.workload == "polar":
+        return run_polar_only(args)
     return run_gb300(args)
 
 
