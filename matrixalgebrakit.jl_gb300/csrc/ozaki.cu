@@ -827,16 +827,31 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
   const int64_t Kpad = ceil_div(Kl > 0 ? Kl : 1, OZ_BK) * OZ_BK;
   const int64_t nkt_total = Kpad / OZ_BK;
   const int64_t tiles = (Mpad / OZ_BM) * (Npad / OZ_BN);
-  // split K so that about two waves of CTAs cover the SMs, whole chunks per split
+  // persistent grid cap: the caller's limit, else the thread's budget, else every SM
+  if (max_ctas <= 0) max_ctas = split_gemm_cta_budget();
+  const int cap = (max_ctas > 0 && max_ctas < num_sms()) ? max_ctas : num_sms();
+  // split K (whole chunks per split) when the tiles alone leave CTAs idle:
+  // the count minimising waves x (chunks per item + the item's fixed cost,
+  // about half a chunk of epilogue), with at most two waves of items so the
+  // partials stay within the measured bound.  A ragged last wave idles the
+  // grid (64 tiles x 3 splits on 152 CTAs: 2 waves at 63 %), so the count is
+  // chosen by the waves it takes, not by the CTAs it would fill.
   int splits = 1;
   {
-    const int sms = num_sms();
     const int64_t nchunk = ceil_div(nkt_total, OZ_KSTEPS_PER_CHUNK);
-    if (tiles < sms) {
-      splits = (int)ceil_div(sms, tiles);
-      if (splits > nchunk) splits = (int)nchunk;
-      if (splits > 32) splits = 32;
-      if (splits < 1) splits = 1;
+    if (tiles < cap && nchunk > 1) {
+      double best = 0.0;
+      for (int s = 1; s <= 32 && s <= nchunk; s++) {
+        const int64_t cps = ceil_div(nchunk, (int64_t)s);
+        const int64_t s_eff = ceil_div(nchunk, cps);
+        const int64_t items = tiles * s_eff;
+        if (s > 1 && items > 2 * (int64_t)cap) break;
+        const double cost = (double)ceil_div(items, (int64_t)cap) * ((double)cps + 0.5);
+        if (s == 1 || cost < best * 0.999) {
+          best = cost;
+          splits = (int)s_eff;
+        }
+      }
     }
   }
   const int64_t chunks_per_split =
@@ -896,8 +911,6 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
                 (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_, part, part ? M * Nl : 0,
                 status};
     const int64_t nwork = (int64_t)tm * tn * splits;
-    if (max_ctas <= 0) max_ctas = split_gemm_cta_budget();
-    const int cap = (max_ctas > 0 && max_ctas < num_sms()) ? max_ctas : num_sms();
     const int grid = (int)(nwork < cap ? nwork : cap);
     note_launch();
     if (nkt_total * OZ_BK <= 128)  // one short chunk: the FFMA conversion
