@@ -78,9 +78,11 @@ typedef struct {
   int32_t maxiter;   /* reference default 10                                  */
   int32_t precision; /* MAK_PREC_NATIVE or MAK_PREC_MIXED                     */
   double tol;        /* > 0: stopping tolerance; 0: reference default
-                        eps(real T)^(2/3); < 0: run exactly maxiter iterations
-                        with no host synchronization (CUDA-graph capturable;
-                        `converged` is reported against the default tol)    */
+                        eps(real T)^(2/3); < 0: no host synchronization
+                        (CUDA-graph capturable): maxiter iterations are
+                        launched and the loop stops on the device once the
+                        default tolerance is met; the stopped iterations'
+                        kernels return at once                              */
 } mak_polar_opts;
 
 /* Options of the pullbacks (reference src/pullbacks/qr.jl:73-77). */
@@ -281,8 +283,10 @@ int mak_right_polar_newton_c(int64_t m, int64_t n, const void* A, int64_t lda, v
  * scheduled longest-first over internal streams that fork from and join back
  * into `stream`, so the whole batch can be captured into a CUDA graph (the
  * internal streams are created by the first call, which must precede any
- * capture).  `infos` is a DEVICE array of nitems records.  Batched polar runs
- * exactly opts->maxiter Newton iterations (no host synchronization).
+ * capture).  `infos` is a DEVICE array of nitems records.  Batched polar
+ * launches opts->maxiter Newton iterations per block and stops each block on
+ * the device once it meets the tolerance (no host synchronization);
+ * infos[i].iterations is the number of steps block i took.
  */
 typedef struct {
   int32_t dtype;    /* MAK_F64 / MAK_C64 / MAK_F32 / MAK_C32                 */

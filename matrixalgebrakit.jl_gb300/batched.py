@@ -82,9 +82,12 @@ def batched_qr_compact(As, alg=None, copy_inputs=True, outs=None, _capturing=Fal
     return outs
 
 
-def batched_left_polar(As, alg=None, copy_inputs=True, outs=None, _capturing=False, **kwargs):
-    """left_polar of every block (fixed Newton iteration count alg.maxiter);
-    returns [(W_i, P_i)]."""
+def batched_left_polar(As, alg=None, copy_inputs=True, outs=None, _capturing=False, _info=None,
+                       **kwargs):
+    """left_polar of every block; returns [(W_i, P_i)].  Without host
+    synchronization (CUDA-graph capturable): alg.maxiter Newton iterations
+    are launched per block and each block stops on the device once it meets
+    the tolerance.  ``_info`` (a list) receives the steps each block took."""
     alg = select_algorithm("left_polar_", None, alg, **kwargs)
     for A in As:
         if A.shape[0] < A.shape[1]:
@@ -94,5 +97,7 @@ def batched_left_polar(As, alg=None, copy_inputs=True, outs=None, _capturing=Fal
                  empty_cm(A.shape[1], A.shape[1], A.dtype, A.device)) for A in As]
     opts = _lib.mak_polar_opts(int(alg.maxiter), PRECISION_CODE[alg.precision],
                                float(alg.tol) if alg.tol is not None else 0.0)
-    _run("polar", As, outs, opts, copy_inputs, _capturing)
+    res = _run("polar", As, outs, opts, copy_inputs, _capturing)
+    if _info is not None and res is not None:
+        _info.extend(int(r.iterations) for r in res)
     return outs

@@ -25,7 +25,8 @@ double split_min_mnk() {
 // C = alpha * sum_s part[s] + beta * C  (fixed summation order)
 template <class T>
 __global__ void splitk_fold_kernel(int64_t M, int64_t N, int splits, const T* part, T alpha,
-                                   T beta, T* C, int64_t ldc) {
+                                   T beta, T* C, int64_t ldc, const int* skip) {
+  if (skipped(skip)) return;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= M * N) return;
   T v = zero_<T>();
@@ -60,7 +61,7 @@ static int gemm_native(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha
   MAK_TRY(gemm<T>(st, M, N, K, one_<T>(), A, B, zero_<T>(), part, M, splits, M * N, &used));
   note_launch();
   splitk_fold_kernel<T><<<(unsigned)ceil_div(M * N, 256), 256, 0, st>>>(M, N, used, part, alpha,
-                                                                       beta, C, ldc);
+                                                                       beta, C, ldc, skip_flag());
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
 

@@ -62,7 +62,8 @@ __device__ __forceinline__ bool is_zero_(T v) { return v == zero_<T>(); }
 template <class T, int BM, int BN, int BK, int TM, int TN>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 gemm_kernel(int M, int N, int K, T alpha, Operand<T> A, Operand<T> B, T beta, T* C,
-            int64_t ldc, int kchunk, int64_t split_stride) {
+            int64_t ldc, int kchunk, int64_t split_stride, const int* skip) {
+  if (skipped(skip)) return;
   constexpr int RX = BM / TM;  // threads along rows
   constexpr int RY = BN / TN;  // threads along columns
   constexpr int NT = RX * RY;
@@ -159,12 +160,14 @@ int gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T> A
     dim3 g((unsigned)ceil_div(M, 32), (unsigned)ceil_div(N, 64), (unsigned)splits);
     note_launch();
     gemm_kernel<T, 32, 64, BK, 2, 4><<<g, 256, 0, st>>>((int)M, (int)N, (int)K, alpha, A, B,
-                                                         beta, C, ldc, kchunk, split_stride);
+                                                         beta, C, ldc, kchunk, split_stride,
+                                                         skip_flag());
   } else {
     dim3 g((unsigned)ceil_div(M, 64), (unsigned)ceil_div(N, 64), (unsigned)splits);
     note_launch();
     gemm_kernel<T, 64, 64, BK, 4, 4><<<g, 256, 0, st>>>((int)M, (int)N, (int)K, alpha, A, B,
-                                                         beta, C, ldc, kchunk, split_stride);
+                                                         beta, C, ldc, kchunk, split_stride,
+                                                         skip_flag());
   }
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }

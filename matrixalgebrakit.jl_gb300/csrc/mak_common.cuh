@@ -321,6 +321,27 @@ int max_smem_optin();
 std::atomic<unsigned long long>& launch_counter();
 inline void note_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
 
+// Device-side stop of a fixed-iteration loop.  While a flag is installed for
+// the calling host thread (SkipScope), the library's heavy kernels launched
+// from that thread take the flag's address and return at once when it is
+// non-zero; the loop's convergence test sets it on the device, so converged
+// iterations cost only their launches and need no host synchronization.
+inline const int*& skip_flag_slot() {
+  static thread_local const int* p = nullptr;
+  return p;
+}
+inline const int* skip_flag() { return skip_flag_slot(); }
+struct SkipScope {
+  const int* prev;
+  explicit SkipScope(const int* f) : prev(skip_flag_slot()) { skip_flag_slot() = f; }
+  ~SkipScope() { skip_flag_slot() = prev; }
+  SkipScope(const SkipScope&) = delete;
+  SkipScope& operator=(const SkipScope&) = delete;
+};
+__device__ __forceinline__ bool skipped(const int* f) {
+  return f != nullptr && *(const volatile int*)f != 0;
+}
+
 // kernel classes timed by the optional profiler (mak_profile_*)
 enum ProfKind {
   PROF_GEMM_NATIVE = 0,  // SIMT FP64/FP32 GEMM (work = flops)

@@ -49,6 +49,7 @@ struct GjArgs {
   unsigned* bar;
   int* status;
   int* singular;
+  const int* skip;  // device stop flag of a fixed-iteration loop (or nullptr)
 };
 
 __device__ __forceinline__ double cabs1_(double x) { return fabs(x); }
@@ -64,6 +65,7 @@ __device__ __forceinline__ void amax_merge(R& v, int& i, R v2, int i2) {
 template <class T>
 __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
   using R = real_t<T>;
+  if (skipped(a.skip)) return;  // the same in every CTA: no barrier is reached
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x b, ld = rpc
   T* fsh = Ps + (size_t)a.rpc * a.b;        // rpc multipliers of the current column
@@ -206,7 +208,8 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
 // Only columns c in [c_lo, c_hi) are touched.
 template <class T>
 __global__ void gje_laswp_save_kernel(int n, T* X, int64_t ldx, int k0, int b, const int* piv,
-                                      T* buf, int c_lo, int c_hi) {
+                                      T* buf, int c_lo, int c_hi, const int* skip) {
+  if (skipped(skip)) return;
   const int c = c_lo + blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= c_hi || (c >= k0 && c < k0 + b)) return;
   T* col = X + (int64_t)c * ldx;
@@ -230,7 +233,8 @@ __global__ void iota_kernel(int n, int* v) {
 }
 
 // iperm = inverse of the composed row permutation
-__global__ void gje_perm_kernel(int n, const int* piv, int* iperm) {
+__global__ void gje_perm_kernel(int n, const int* piv, int* iperm, const int* skip) {
+  if (skipped(skip)) return;
   extern __shared__ int perm[];
   for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
   __syncthreads();
@@ -330,7 +334,7 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
         (int64_t)per_sm * sms < G)
       return MAK_ERR_UNSUPPORTED;
     GjArgs<T> ga{X, ldx, (int)n, (int)k0, b, (int)rpc, piv, part_val, part_idx, swapbuf,
-                 cand, sms, bar, &info->status, &info->singular};
+                 cand, sms, bar, &info->status, &info->singular, skip_flag()};
     void* args[] = {&ga};
     ProfScope prof(s, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
     note_launch();
@@ -347,7 +351,7 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
       MAK_TRY(panel(k0, b, s, max_ctas));
       note_launch();
       gje_laswp_save_kernel<T><<<(unsigned)ceil_div(c_hi - c_lo, 128), 128, 0, s>>>(
-          (int)n, X, ldx, (int)k0, b, piv, buf, (int)c_lo, (int)c_hi);
+          (int)n, X, ldx, (int)k0, b, piv, buf, (int)c_lo, (int)c_hi, skip_flag());
       MAK_CUDA_TRY(cudaGetLastError());
       const T* F = X + k0 * ldx;
       if (k0 > c_lo)
@@ -366,7 +370,7 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
     if (c_hi <= c_lo) return 0;
     note_launch();
     gje_laswp_save_kernel<T><<<(unsigned)ceil_div(c_hi - c_lo, 128), 128, 0, s>>>(
-        (int)n, X, ldx, (int)K0, (int)KB, piv, bufo, (int)c_lo, (int)c_hi);
+        (int)n, X, ldx, (int)K0, (int)KB, piv, bufo, (int)c_lo, (int)c_hi, skip_flag());
     MAK_CUDA_TRY(cudaGetLastError());
     const T* Fb = X + K0 * ldx;
     const int64_t l1 = c_hi < K0 ? c_hi : K0;  // left part [c_lo, l1)
@@ -419,7 +423,7 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
     }
   }
   note_launch();
-  gje_perm_kernel<<<1, 1024, (size_t)n * sizeof(int), st>>>((int)n, piv, iperm);
+  gje_perm_kernel<<<1, 1024, (size_t)n * sizeof(int), st>>>((int)n, piv, iperm, skip_flag());
   MAK_CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -439,7 +443,9 @@ __global__ void __launch_bounds__(256) newton_update_kernel(int n, T* X, int64_t
                                                             const T* Xi, int64_t ldi,
                                                             const int* iperm,
                                                             const real_t<T>* nrm2,
-                                                            real_t<T>* conv) {
+                                                            real_t<T>* conv,
+                                                            const int* skip) {
+  if (skipped(skip)) return;
   using R = real_t<T>;
   __shared__ T t[32][33];
   __shared__ R sh[32];
@@ -466,12 +472,23 @@ __global__ void __launch_bounds__(256) newton_update_kernel(int n, T* X, int64_t
   if (threadIdx.x == 0) atomic_max_nonneg(conv, dmax);
 }
 
+// Fixed-iteration mode: after each Newton step, count it and stop the loop
+// on the device once its measure is within tol (or is not a number), as the
+// reference's host loop does; later iterations' kernels see the flag.
+template <class R>
+__global__ void newton_stop_kernel(const R* conv, R tol, int* stopw, R* conv_last) {
+  if (stopw[0]) return;
+  stopw[1] += 1;
+  *conv_last = *conv;
+  if (!(*conv > tol)) stopw[0] = 1;
+}
+
 template <class T>
-__global__ void info_polar_dev_kernel(mak_info* info, int it, const real_t<T>* conv,
-                                      real_t<T> tol) {
-  info->iterations = it;
-  info->residual = (double)*conv;
-  info->converged = (*conv <= tol) ? 1 : 0;
+__global__ void info_polar_fixed_kernel(mak_info* info, const int* stopw,
+                                        const real_t<T>* conv_last, real_t<T> tol) {
+  info->iterations = stopw[1];
+  info->residual = (double)*conv_last;
+  info->converged = (*conv_last <= tol) ? 1 : 0;
 }
 
 template <class T>
@@ -491,6 +508,7 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
   T* Y = ar.take<T>((size_t)n * n + 1);
   int* iperm = ar.take<int>(n + 1);
   R* red = ar.take<R>(RED_CTAS + 8);
+  int* stopw = ar.take<int>(2);  // fixed-iteration mode: [0] stop flag, [1] steps taken
   T* Qw = (m > n) ? ar.take<T>((size_t)m * n) : nullptr;
   T* Rw = (m > n) ? ar.take<T>((size_t)n * n) : nullptr;
   T* A0 = (m == n && want_p) ? ar.take<T>((size_t)n * n) : nullptr;
@@ -515,8 +533,8 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
     }
   }
   const size_t tail_bytes = qr_ws > gj_ws ? qr_ws : gj_ws;
-  // tol < 0: run exactly maxiter iterations with no host synchronization
-  // (graph-capturable; |tol| still decides the reported convergence flag)
+  // tol < 0: no host synchronization (graph-capturable); the loop launches
+  // maxiter iterations and stops on the device once |tol| is reached
   const bool fixed_iters = tol < 0;
   if (fixed_iters) tol = -tol;
   char* tail = ar.take<char>(tail_bytes);
@@ -524,6 +542,7 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
   R* nrm2 = red + RED_CTAS;      // [0] ||X||^2, [1] ||Xi||^2
   R* conv = red + RED_CTAS + 2;  // max |D|
+  R* conv_last = red + RED_CTAS + 3;
 
   if (m > n) {
     Arena sub(tail, tail_bytes);
@@ -536,32 +555,44 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
   int it = 0;
   R hconv = R(0);
   bool converged = (n == 0);
-  for (it = 1; it <= maxiter && n > 0; it++) {
-    MAK_TRY(copy_mat<T>(st, n, n, X, n, Y, n));
-    {
-      Arena sub(tail, tail_bytes);
-      MAK_TRY(gje_inverse<T>(st, n, Y, n, iperm, precision, sub, info));
-    }
-    MAK_TRY(reduce_mat<T>(st, n, n, X, n, 0, red, nrm2));
-    MAK_TRY(reduce_mat<T>(st, n, n, Y, n, 0, red, nrm2 + 1));
-    MAK_CUDA_TRY(cudaMemsetAsync(conv, 0, sizeof(R), st));
-    dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
-    note_launch();
-    newton_update_kernel<T><<<g, 256, 0, st>>>((int)n, X, n, Y, n, iperm, nrm2, conv);
-    MAK_CUDA_TRY(cudaGetLastError());
-    if (!fixed_iters) {
-      MAK_CUDA_TRY(cudaMemcpyAsync(&hconv, conv, sizeof(R), cudaMemcpyDeviceToHost, st));
-      MAK_CUDA_TRY(cudaStreamSynchronize(st));
-      if (!(hconv > (R)tol)) {  // also stops on NaN
-        converged = hconv <= (R)tol;
-        break;
+  if (fixed_iters) {
+    MAK_CUDA_TRY(cudaMemsetAsync(stopw, 0, 2 * sizeof(int), st));
+    MAK_CUDA_TRY(cudaMemsetAsync(conv_last, 0, sizeof(R), st));
+  }
+  {  // the device stop flag applies to the iterations only
+    SkipScope stop_scope(fixed_iters ? stopw : nullptr);
+    for (it = 1; it <= maxiter && n > 0; it++) {
+      MAK_TRY(copy_mat<T>(st, n, n, X, n, Y, n));
+      {
+        Arena sub(tail, tail_bytes);
+        MAK_TRY(gje_inverse<T>(st, n, Y, n, iperm, precision, sub, info));
+      }
+      MAK_TRY(reduce_mat<T>(st, n, n, X, n, 0, red, nrm2));
+      MAK_TRY(reduce_mat<T>(st, n, n, Y, n, 0, red, nrm2 + 1));
+      MAK_CUDA_TRY(cudaMemsetAsync(conv, 0, sizeof(R), st));
+      dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+      note_launch();
+      newton_update_kernel<T><<<g, 256, 0, st>>>((int)n, X, n, Y, n, iperm, nrm2, conv,
+                                                 skip_flag());
+      MAK_CUDA_TRY(cudaGetLastError());
+      if (fixed_iters) {
+        note_launch();
+        newton_stop_kernel<R><<<1, 1, 0, st>>>(conv, (R)tol, stopw, conv_last);
+        MAK_CUDA_TRY(cudaGetLastError());
+      } else {
+        MAK_CUDA_TRY(cudaMemcpyAsync(&hconv, conv, sizeof(R), cudaMemcpyDeviceToHost, st));
+        MAK_CUDA_TRY(cudaStreamSynchronize(st));
+        if (!(hconv > (R)tol)) {  // also stops on NaN
+          converged = hconv <= (R)tol;
+          break;
+        }
       }
     }
   }
   if (it > maxiter) it = maxiter;
   note_launch();
   if (fixed_iters)
-    info_polar_dev_kernel<T><<<1, 1, 0, st>>>(info, n > 0 ? maxiter : 0, conv, (R)tol);
+    info_polar_fixed_kernel<T><<<1, 1, 0, st>>>(info, stopw, conv_last, (R)tol);
   else
     info_polar_kernel<T><<<1, 1, 0, st>>>(info, n > 0 ? it : 0, (double)hconv, converged ? 1 : 0);
   MAK_CUDA_TRY(cudaGetLastError());

@@ -70,3 +70,22 @@ def test_batched_graph_capture(mak, cuda):
     torch.cuda.synchronize()
     for A, (Q, R) in zip(blocks, outs):
         assert O.rel_err(to_host(R), O.qr_compact(A)[1]) <= 1e-12
+
+
+def test_batched_polar_stops_on_device(mak, cuda):
+    """The batch launches maxiter Newton iterations per block without a host
+    synchronization, and each block stops on the device at the reference's
+    criterion (conv <= tol): it takes the same number of steps, and gives
+    the same factors, as the host-checked single-block call."""
+    blocks = _blocks(76, 12, 240)
+    iters = []
+    outs = mak.batched_left_polar([to_dev(A, cuda) for A in blocks], maxiter=30, _info=iters)
+    assert len(iters) == len(blocks)
+    for A, (W, P), k in zip(blocks, outs, iters):
+        info = {}
+        W1, P1 = mak.left_polar_(to_dev(A, cuda), None, mak.GB300_PolarNewton(maxiter=30),
+                                 _info=info)
+        assert info["converged"] and k == info["iterations"] < 30
+        assert O.rel_err(to_host(W), to_host(W1)) <= 1e-14
+        assert O.rel_err(to_host(P), to_host(P1)) <= 1e-14
+        assert np.linalg.norm(A - to_host(W) @ to_host(P)) / np.linalg.norm(A) <= 1e-13
