@@ -10,7 +10,7 @@
 namespace mak {
 
 double split_min_mnk() {
-  static double v = 67108864.0;  // 2^26
+  static double v = 4194304.0;  // 2^22
   static std::once_flag f;
   std::call_once(f, [] {
     const char* e = getenv("MAK_SPLIT_MIN_MNK");

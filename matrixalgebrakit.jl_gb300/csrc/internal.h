@@ -72,9 +72,9 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
 // C-ABI GEMM, whose caller chose the arithmetic explicitly).
 constexpr int PREC_SPLIT_ALWAYS = 3;
 // Inside the factorizations, MAK_PREC_MIXED splits products with at least
-// split_min_mnk() multiply-adds (complex counted 4x; 2^26 by default,
+// split_min_mnk() multiply-adds (complex counted 4x; 2^22 by default,
 // MAK_SPLIT_MIN_MNK overrides it, read once); smaller ones stay native.  The
-// mixed blockings of QR and Gauss-Jordan are gated by the same value.
+// QR's mixed blocking is gated by the same value (Gauss-Jordan's has its own).
 double split_min_mnk();
 
 // Dispatch: the tensor-core split GEMM when `precision` is MAK_PREC_MIXED and

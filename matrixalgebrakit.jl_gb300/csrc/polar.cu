@@ -280,10 +280,11 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
   // adds, complex counted 4x: n >= 2048 real, n >= 1024 complex); below that
   // its extra launches and split passes cost more than the tensor cores
   // save (measured on batches of blocks with n <= 1024), and the native
-  // elimination runs even when mixed precision is asked for
+  // elimination runs even when mixed precision is asked for (a gate of its
+  // own: the general split-product gate does not move it)
   const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8 &&
                      (traits<T>::cpx ? 4.0 : 1.0) * (double)n * (double)n * GJ_OUTER_NB >=
-                         8.0 * split_min_mnk();
+                         536870912.0;  // 2^29
   const int NBO = mixed ? GJ_OUTER_NB : GJ_NB;
   int* piv = ar.take<int>(n > 0 ? n : 1);
   // per-CTA pivot partials and candidate rows, double-buffered by column parity
