@@ -189,8 +189,10 @@ int mak_lq_full_c(int64_t m, int64_t n, const void* A, int64_t lda, void* L, int
  * Same arguments, results and errors as mak_qr_compact_d without the
  * workspace; its scratch is one fixed device array of
  * MAK_QR_NOALLOC_SCRATCH_BYTES inside the library.
- *  - A problem whose mak_qr_workspace size exceeds that array is rejected
- *    with MAK_ERR_WORKSPACE before any work is queued.
+ *  - With MAK_PREC_MIXED, a problem whose split products' planes do not fit
+ *    the array runs the native blocking instead (both are FP64-accurate).
+ *    A problem whose native mak_qr_workspace size exceeds the array is
+ *    rejected with MAK_ERR_WORKSPACE before any work is queued.
  *  - The first call on each device (made with that device current) looks up
  *    the array's address; it must come before any stream capture starts on
  *    that device.

@@ -9,8 +9,11 @@
 // file-scope device array, so the call itself allocates nothing (no
 // cudaMalloc / cudaFree, no allocating library routine).
 //
-// * The array's size is fixed at MAK_QR_NOALLOC_SCRATCH_BYTES (32 MiB).  A
-//   problem whose workspace (mak_qr_workspace) exceeds it is rejected with
+// * The array's size is fixed at MAK_QR_NOALLOC_SCRATCH_BYTES (32 MiB).  When
+//   mixed precision is asked for and the split products' planes do not fit,
+//   the call runs the native blocking instead (both are FP64-accurate; the
+//   precision option chooses speed, not accuracy).  A problem whose native
+//   workspace (mak_qr_workspace) exceeds the array as well is rejected with
 //   MAK_ERR_WORKSPACE before any work is queued.
 // * Set-up, once per device: the first call made while a device is current
 //   looks up the array's device address with cudaGetSymbolAddress (this is
@@ -67,13 +70,19 @@ extern "C" int mak_qr_compact_d_noalloc(int64_t m, int64_t n, double* A, int64_t
   size_t need = 0;
   const int rq = mak_qr_workspace(MAK_F64, m, n, 0, opts, &need);
   if (rq != 0) return rq;
+  mak_qr_opts o{1, 0, MAK_PREC_NATIVE, 0};
+  if (opts) o = *opts;
+  if (need > QR_NOALLOC_SCRATCH_BYTES && o.precision == MAK_PREC_MIXED) {
+    o.precision = MAK_PREC_NATIVE;  // the split planes do not fit: the native blocking
+    if (mak_qr_workspace(MAK_F64, m, n, 0, &o, &need) != 0) return MAK_ERR_WORKSPACE;
+  }
   if (need > QR_NOALLOC_SCRATCH_BYTES) return MAK_ERR_WORKSPACE;
   void* scratch = nullptr;
   MAK_TRY(noalloc_scratch(&scratch));
   // the look-ahead path creates its side stream on first use: keep it off
   const bool la = lookahead_enabled();
   set_lookahead(false);
-  const int rc = mak_qr_compact_d(m, n, A, lda, Q, ldq, R, ldr, opts, scratch,
+  const int rc = mak_qr_compact_d(m, n, A, lda, Q, ldq, R, ldr, &o, scratch,
                                   QR_NOALLOC_SCRATCH_BYTES, info, stream);
   set_lookahead(la);
   return rc;

@@ -80,6 +80,7 @@ struct OzArgs {
   double* part;             // split-K partials (nullptr: write C directly), split z at
   int64_t part_stride;      //   part + z * part_stride
   int* status;
+  const int* skip;          // device stop flag of a fixed-iteration loop (or nullptr)
 };
 
 // One work item of the persistent loop: an output tile and a K range.
@@ -301,6 +302,8 @@ template <int S, int CHUNK>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
 oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                OzArgs a) {
+  // a stopped iteration: every CTA leaves before any barrier or TMEM set-up
+  if (skipped(a.skip)) return;
   constexpr int A_TILE = OZ_BM * OZ_ROW_BYTES;  // bytes per A-plane tile
   constexpr int B_TILE = OZ_BN * OZ_ROW_BYTES;  // bytes per B-plane tile
   constexpr int STAGE = S * (A_TILE + B_TILE);
@@ -563,7 +566,8 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 // split-K fold: C = alpha * sum_s part[s] + beta * C  (fixed order)
 __global__ void oz_reduce_kernel(int M, int Nl, int splits, const double* part, int64_t stride,
                                  double* C, int64_t ldc, int cpx, int Nc, double alpha,
-                                 double beta) {
+                                 double beta, const int* skip) {
+  if (skipped(skip)) return;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (int64_t)M * Nl) return;
   const int gi = (int)(e % M), gj = (int)(e / M);
@@ -633,7 +637,9 @@ __device__ __forceinline__ int exp_of_absbits(unsigned long long b) {
 constexpr int OZ_EXP_KCHUNK = 1024;
 template <class T>
 __global__ void __launch_bounds__(256) oz_absmax_kernel(OzSrc<T> s, int R, int K,
-                                                        unsigned long long* mx_bits) {
+                                                        unsigned long long* mx_bits,
+                                                        const int* skip) {
+  if (skipped(skip)) return;
   const int k0 = blockIdx.y * OZ_EXP_KCHUNK;
   const int k1 = min(K, k0 + OZ_EXP_KCHUNK);
   if (oz_contig_r(s)) {
@@ -664,7 +670,9 @@ __global__ void __launch_bounds__(256) oz_absmax_kernel(OzSrc<T> s, int R, int K
     if (lane == 0 && mx) atomicMax(&mx_bits[r], mx);
   }
 }
-__global__ void oz_exp_from_bits_kernel(int R, const unsigned long long* mx_bits, int* E) {
+__global__ void oz_exp_from_bits_kernel(int R, const unsigned long long* mx_bits, int* E,
+                                        const int* skip) {
+  if (skipped(skip)) return;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < R) E[r] = exp_of_absbits(mx_bits[r]);
 }
@@ -675,9 +683,9 @@ static int oz_exponents(cudaStream_t st, const OzSrc<T>& s, int R, int K, unsign
   const unsigned gy = (unsigned)ceil_div(K > 0 ? K : 1, OZ_EXP_KCHUNK);
   const unsigned gx = (unsigned)(oz_contig_r(s) ? ceil_div(R, 256) : ceil_div(R, 8));
   note_launch();
-  oz_absmax_kernel<T><<<dim3(gx, gy), 256, 0, st>>>(s, R, K, bits);
+  oz_absmax_kernel<T><<<dim3(gx, gy), 256, 0, st>>>(s, R, K, bits, skip_flag());
   note_launch();
-  oz_exp_from_bits_kernel<<<(unsigned)ceil_div(R, 256), 256, 0, st>>>(R, bits, E);
+  oz_exp_from_bits_kernel<<<(unsigned)ceil_div(R, 256), 256, 0, st>>>(R, bits, E, skip_flag());
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
 
@@ -685,7 +693,8 @@ static int oz_exponents(cudaStream_t st, const OzSrc<T>& s, int R, int K, unsign
 template <class T, int S>
 __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> s, int R, int K, int Rpad,
                                                        int Kpad, const int* E,
-                                                       __nv_bfloat16* planes) {
+                                                       __nv_bfloat16* planes, const int* skip) {
+  if (skipped(skip)) return;
   __shared__ double tile[64][65];
   __shared__ unsigned short lut[129];  // bf16 bits of the integers -64 .. 64
   const int r0 = blockIdx.y * 64, k0 = blockIdx.x * 64;
@@ -888,10 +897,12 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
   MAK_TRY(oz_exponents<T>(st, sb, (int)Nl, (int)Kl, bitsB, EB));
   note_launch();
   oz_split_kernel<T, S><<<dim3((unsigned)(Kpad / 64 + (Kpad % 64 ? 1 : 0)), (unsigned)(Mpad / 64)),
-                          256, 0, st>>>(sa, (int)M, (int)Kl, (int)Mpad, (int)Kpad, EA, PA);
+                          256, 0, st>>>(sa, (int)M, (int)Kl, (int)Mpad, (int)Kpad, EA, PA,
+                                           skip_flag());
   note_launch();
   oz_split_kernel<T, S><<<dim3((unsigned)(Kpad / 64 + (Kpad % 64 ? 1 : 0)), (unsigned)(Npad / 64)),
-                          256, 0, st>>>(sb, (int)Nl, (int)Kl, (int)Npad, (int)Kpad, EB, PB);
+                          256, 0, st>>>(sb, (int)Nl, (int)Kl, (int)Npad, (int)Kpad, EB, PB,
+                                           skip_flag());
   MAK_CUDA_TRY(cudaGetLastError());
 
   CUtensorMap mapA, mapB;
@@ -909,7 +920,7 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
     const int tm = (int)(Mpad / OZ_BM), tn = (int)(Npad / OZ_BN);
     OzArgs args{(int)M, (int)Nl, (int)nkt_total, split_steps, tm, tn, splits, EA, EB,
                 (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_, part, part ? M * Nl : 0,
-                status};
+                status, skip_flag()};
     const int64_t nwork = (int64_t)tm * tn * splits;
     const int grid = (int)(nwork < cap ? nwork : cap);
     note_launch();
@@ -922,7 +933,8 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
   if (part) {
     note_launch();
     oz_reduce_kernel<<<(unsigned)ceil_div(M * Nl, 256), 256, 0, st>>>(
-        (int)M, (int)Nl, splits, part, M * Nl, (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_);
+        (int)M, (int)Nl, splits, part, M * Nl, (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_,
+        skip_flag());
     MAK_CUDA_TRY(cudaGetLastError());
   }
   return 0;

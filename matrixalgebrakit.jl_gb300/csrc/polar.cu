@@ -473,15 +473,62 @@ __global__ void __launch_bounds__(256) newton_update_kernel(int n, T* X, int64_t
   if (threadIdx.x == 0) atomic_max_nonneg(conv, dmax);
 }
 
-// Fixed-iteration mode: after each Newton step, count it and stop the loop
-// on the device once its measure is within tol (or is not a number), as the
-// reference's host loop does; later iterations' kernels see the flag.
+// Newton-Schulz finish (mixed precision, Float64 types): once a Newton step
+// measured n * max|D| <= 1/2 (so ||D||_2 <= ||D||_F <= 1/2 and the new
+// iterate's singular values lie in [1, 1.05]), the iteration continues with
+// X <- X (3 I - X^H X) / 2, two products on the split tensor-core path
+// instead of a latency-bound Gauss-Jordan inverse; it converges
+// quadratically there (error e -> 1.5 e^2).  Its measure 2 max|dX| is on the
+// Newton step's scale (max|D| = 2 max|dX|) and meets the same tolerance.
+constexpr double NS_SWITCH = 0.5;  // n * max|D| at which Newton-Schulz takes over
+
+// Z <- 1.5 I - 0.5 Z  (n x n, ld n)
+template <class T>
+__global__ void ns_prepare_kernel(int n, T* Z, const int* skip) {
+  if (skipped(skip)) return;
+  using R = real_t<T>;
+  const int64_t nn = (int64_t)n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % n, j = e / n;
+    const T d = (i == j) ? make_scalar<T>(R(1.5), R(0)) : zero_<T>();
+    Z[e] = d - R(0.5) * Z[e];
+  }
+}
+
+// X <- Xn and *conv = max(*conv, 2 max|Xn - X|)
+template <class T>
+__global__ void __launch_bounds__(256) ns_update_kernel(int64_t nn, T* X, const T* Xn,
+                                                        real_t<T>* conv, const int* skip) {
+  if (skipped(skip)) return;
+  using R = real_t<T>;
+  __shared__ R sh[32];
+  R dmax = R(0);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const T xn = Xn[e];
+    dmax = fmax(dmax, abs_(xn - X[e]));
+    X[e] = xn;
+  }
+  dmax = block_max(dmax, sh);
+  if (threadIdx.x == 0) atomic_max_nonneg(conv, R(2) * dmax);
+}
+
+// Fixed-iteration mode: after each step, count it and stop the loop on the
+// device once its measure is within tol (or is not a number), as the
+// reference's host loop does; the Newton-Schulz switch is decided here too.
+// w: [0] stopped, [1] steps taken, [2] Newton-Schulz phase, [3] skip flag of
+// the Newton step's kernels, [4] skip flag of the Newton-Schulz step's.
 template <class R>
-__global__ void newton_stop_kernel(const R* conv, R tol, int* stopw, R* conv_last) {
-  if (stopw[0]) return;
-  stopw[1] += 1;
+__global__ void newton_stop_kernel(const R* conv, R tol, int* w, R* conv_last, int n,
+                                   int ns_ok) {
+  if (w[0]) return;
+  w[1] += 1;
   *conv_last = *conv;
-  if (!(*conv > tol)) stopw[0] = 1;
+  if (!(*conv > tol)) w[0] = 1;
+  else if (ns_ok && !w[2] && (R)n * *conv <= (R)NS_SWITCH) w[2] = 1;
+  w[3] = w[0] | w[2];
+  w[4] = w[0] | !w[2];
 }
 
 template <class T>
@@ -509,7 +556,18 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
   T* Y = ar.take<T>((size_t)n * n + 1);
   int* iperm = ar.take<int>(n + 1);
   R* red = ar.take<R>(RED_CTAS + 8);
-  int* stopw = ar.take<int>(2);  // fixed-iteration mode: [0] stop flag, [1] steps taken
+  int* stopw = ar.take<int>(5);  // fixed-iteration mode: see newton_stop_kernel
+  const bool ns_ok = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8;
+  T* Yn = ns_ok ? ar.take<T>((size_t)n * n + 1) : nullptr;  // Newton-Schulz product
+  // Without host synchronization (the batched driver) both step kinds are
+  // launched every iteration and flags let one run.  There the finish pays
+  // only for 256 <= n <= 384 (measured): below, the extra launches cost more
+  // than the Gauss-Jordan inverses saved; above, its two split products under
+  // the batch's per-stream CTA budget cost about an inverse each and hold
+  // their SMs against the other streams' panels, while the finish takes one
+  // step more than Newton from the switch point.  The host-checked loop
+  // launches just the step it takes and uses the finish at every n.
+  const bool ns_fixed_ok = ns_ok && n >= 256 && n <= 384;
   T* Qw = (m > n) ? ar.take<T>((size_t)m * n) : nullptr;
   T* Rw = (m > n) ? ar.take<T>((size_t)n * n) : nullptr;
   T* A0 = (m == n && want_p) ? ar.take<T>((size_t)n * n) : nullptr;
@@ -557,37 +615,76 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
   R hconv = R(0);
   bool converged = (n == 0);
   if (fixed_iters) {
-    MAK_CUDA_TRY(cudaMemsetAsync(stopw, 0, 2 * sizeof(int), st));
+    MAK_CUDA_TRY(cudaMemsetAsync(stopw, 0, 4 * sizeof(int), st));
+    MAK_CUDA_TRY(cudaMemsetAsync(stopw + 4, 1, sizeof(int), st));  // non-zero: Newton first
     MAK_CUDA_TRY(cudaMemsetAsync(conv_last, 0, sizeof(R), st));
   }
-  {  // the device stop flag applies to the iterations only
-    SkipScope stop_scope(fixed_iters ? stopw : nullptr);
-    for (it = 1; it <= maxiter && n > 0; it++) {
-      MAK_TRY(copy_mat<T>(st, n, n, X, n, Y, n));
+  const int64_t nn = n * n;
+  const unsigned gnn = (unsigned)(ceil_div(nn > 0 ? nn : 1, (int64_t)256) < RED_CTAS
+                                      ? ceil_div(nn > 0 ? nn : 1, (int64_t)256)
+                                      : RED_CTAS);
+  // one Newton step: X <- (g X + X^{-H}/g) / 2, measure max|D| into conv
+  auto newton_step = [&]() -> int {
+    MAK_TRY(copy_mat<T>(st, n, n, X, n, Y, n));
+    {
+      Arena sub(tail, tail_bytes);
+      MAK_TRY(gje_inverse<T>(st, n, Y, n, iperm, precision, sub, info));
+    }
+    MAK_TRY(reduce_mat<T>(st, n, n, X, n, 0, red, nrm2));
+    MAK_TRY(reduce_mat<T>(st, n, n, Y, n, 0, red, nrm2 + 1));
+    dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+    note_launch();
+    newton_update_kernel<T><<<g, 256, 0, st>>>((int)n, X, n, Y, n, iperm, nrm2, conv,
+                                               skip_flag());
+    return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+  };
+  // one Newton-Schulz step: X <- X (3 I - X^H X) / 2 (Y holds X^H X, then
+  // 1.5 I - 0.5 X^H X), measure 2 max|dX| into conv
+  auto ns_step = [&]() -> int {
+    {
+      Arena oz(tail, tail_bytes);
+      MAK_TRY(gemm_prec<T>(st, precision, n, n, n, one_<T>(), opnd<T>(X, n, OP_C), opnd<T>(X, n),
+                           zero_<T>(), Y, n, oz, &info->status));
+    }
+    note_launch();
+    ns_prepare_kernel<T><<<gnn, 256, 0, st>>>((int)n, Y, skip_flag());
+    MAK_CUDA_TRY(cudaGetLastError());
+    {
+      Arena oz(tail, tail_bytes);
+      MAK_TRY(gemm_prec<T>(st, precision, n, n, n, one_<T>(), opnd<T>(X, n), opnd<T>(Y, n),
+                           zero_<T>(), Yn, n, oz, &info->status));
+    }
+    note_launch();
+    ns_update_kernel<T><<<gnn, 256, 0, st>>>(nn, X, Yn, conv, skip_flag());
+    return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+  };
+  bool in_ns = false;  // tolerance mode: the host decides the phase
+  for (it = 1; it <= maxiter && n > 0; it++) {
+    MAK_CUDA_TRY(cudaMemsetAsync(conv, 0, sizeof(R), st));
+    if (fixed_iters) {
+      // both step kinds are launched; device flags let exactly one run (and
+      // neither once the loop has stopped)
       {
-        Arena sub(tail, tail_bytes);
-        MAK_TRY(gje_inverse<T>(st, n, Y, n, iperm, precision, sub, info));
+        SkipScope skip_newton(stopw + 3);
+        MAK_TRY(newton_step());
       }
-      MAK_TRY(reduce_mat<T>(st, n, n, X, n, 0, red, nrm2));
-      MAK_TRY(reduce_mat<T>(st, n, n, Y, n, 0, red, nrm2 + 1));
-      MAK_CUDA_TRY(cudaMemsetAsync(conv, 0, sizeof(R), st));
-      dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+      if (ns_fixed_ok) {
+        SkipScope skip_ns(stopw + 4);
+        MAK_TRY(ns_step());
+      }
       note_launch();
-      newton_update_kernel<T><<<g, 256, 0, st>>>((int)n, X, n, Y, n, iperm, nrm2, conv,
-                                                 skip_flag());
+      newton_stop_kernel<R><<<1, 1, 0, st>>>(conv, (R)tol, stopw, conv_last, (int)n,
+                                             ns_fixed_ok ? 1 : 0);
       MAK_CUDA_TRY(cudaGetLastError());
-      if (fixed_iters) {
-        note_launch();
-        newton_stop_kernel<R><<<1, 1, 0, st>>>(conv, (R)tol, stopw, conv_last);
-        MAK_CUDA_TRY(cudaGetLastError());
-      } else {
-        MAK_CUDA_TRY(cudaMemcpyAsync(&hconv, conv, sizeof(R), cudaMemcpyDeviceToHost, st));
-        MAK_CUDA_TRY(cudaStreamSynchronize(st));
-        if (!(hconv > (R)tol)) {  // also stops on NaN
-          converged = hconv <= (R)tol;
-          break;
-        }
+    } else {
+      MAK_TRY(in_ns ? ns_step() : newton_step());
+      MAK_CUDA_TRY(cudaMemcpyAsync(&hconv, conv, sizeof(R), cudaMemcpyDeviceToHost, st));
+      MAK_CUDA_TRY(cudaStreamSynchronize(st));
+      if (!(hconv > (R)tol)) {  // also stops on NaN
+        converged = hconv <= (R)tol;
+        break;
       }
+      if (ns_ok && !in_ns && (R)n * hconv <= (R)NS_SWITCH) in_ns = true;
     }
   }
   if (it > maxiter) it = maxiter;

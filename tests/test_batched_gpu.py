@@ -72,20 +72,28 @@ def test_batched_graph_capture(mak, cuda):
         assert O.rel_err(to_host(R), O.qr_compact(A)[1]) <= 1e-12
 
 
-def test_batched_polar_stops_on_device(mak, cuda):
-    """The batch launches maxiter Newton iterations per block without a host
+@pytest.mark.parametrize("precision", ["native", "mixed"])
+def test_batched_polar_stops_on_device(mak, cuda, precision):
+    """The batch launches maxiter iterations per block without a host
     synchronization, and each block stops on the device at the reference's
-    criterion (conv <= tol): it takes the same number of steps, and gives
-    the same factors, as the host-checked single-block call."""
+    criterion (conv <= tol), switching to the Newton-Schulz finish in mixed
+    precision: it takes the same number of steps, and gives the same
+    factors, as the host-checked single-block call (mixed: the batch caps
+    the split product's grid, which changes its K-split rounding, so +-1
+    step and 1e-13)."""
     blocks = _blocks(76, 12, 240)
     iters = []
-    outs = mak.batched_left_polar([to_dev(A, cuda) for A in blocks], maxiter=30, _info=iters)
+    alg = mak.GB300_PolarNewton(maxiter=30, precision=precision)
+    outs = mak.batched_left_polar([to_dev(A, cuda) for A in blocks], alg, _info=iters)
     assert len(iters) == len(blocks)
+    exact = precision == "native"
     for A, (W, P), k in zip(blocks, outs, iters):
         info = {}
-        W1, P1 = mak.left_polar_(to_dev(A, cuda), None, mak.GB300_PolarNewton(maxiter=30),
-                                 _info=info)
-        assert info["converged"] and k == info["iterations"] < 30
-        assert O.rel_err(to_host(W), to_host(W1)) <= 1e-14
-        assert O.rel_err(to_host(P), to_host(P1)) <= 1e-14
+        W1, P1 = mak.left_polar_(to_dev(A, cuda), None, alg, _info=info)
+        assert info["converged"] and info["iterations"] < 30
+        assert (k == info["iterations"]) if exact else abs(k - info["iterations"]) <= 1
+        tol = 1e-14 if exact else 1e-13
+        assert O.rel_err(to_host(W), to_host(W1)) <= tol
+        assert O.rel_err(to_host(P), to_host(P1)) <= tol
         assert np.linalg.norm(A - to_host(W) @ to_host(P)) / np.linalg.norm(A) <= 1e-13
+        assert O.orth_error(to_host(W)) <= 1e-12
