@@ -1,7 +1,8 @@
 """Batched entry points over many uneven blocks (block-sparse symmetry sectors).
 
 The reference has no batched API -- a caller loops ``qr_compact!`` /
-``left_polar!`` over the blocks.  ``batched_qr_compact`` and
+``left_polar!`` over the blocks (the symmetry sectors of a block-sparse tensor,
+the tensors of an orthogonalisation sweep).  ``batched_qr_compact`` and
 ``batched_left_polar`` take the whole list in one stream-ordered call
 (mak_batched_*), with longest-first scheduling over internal streams; the
 result is identical to the per-block calls.

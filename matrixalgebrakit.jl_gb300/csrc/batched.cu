@@ -2,7 +2,8 @@
 // sectors of a block-sparse tensor), GB300 native.
 //
 // The reference has no batched API: a caller loops over blocks and calls
-// qr_compact! / left_polar! once per block (SURVEY: C3 / C5 workloads).  Here
+// qr_compact! / left_polar! once per block (the symmetry sectors of a
+// block-sparse tensor, an orthogonalisation sweep).  Here
 // one call takes the whole work list:
 //  * blocks are ordered by estimated flops (longest first) and dealt to the
 //    least-loaded of BATCH_STREAMS internal streams (LPT schedule), so large

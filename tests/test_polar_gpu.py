@@ -3,7 +3,7 @@
 Oracle: the reference's PolarNewton restated (and PolarViaSVD, the
 reference's default) on the CPU.  The polar factor of a matrix with
 condition number k is itself only determined to ~k * eps, so W and P are
-compared at 1e-10 relative (well-conditioned inputs) and the BASELINE
+compared at 1e-10 relative (well-conditioned inputs) and the accuracy
 bounds are checked directly: ||A - W P||/||A|| <= 1e-12 and
 ||W^H W - I|| <= 1e-12 in Float64.  Float32: 1e-4 relative.
 """
@@ -116,7 +116,8 @@ def test_left_polar_errors_and_warning(mak, cuda):
 @pytest.mark.parametrize("shape", [(300, 300), (700, 260), (512, 512), (768, 768)])
 def test_left_polar_mixed(mak, cuda, dt, shape):
     """precision="mixed": 128-wide Gauss-Jordan blocks and the Newton/QR
-    products on the split-precision tensor-core GEMM; BASELINE bounds."""
+    products on the split-precision tensor-core GEMM (with the Newton-Schulz
+    finish); the 1e-12 accuracy bounds."""
     rng = np.random.default_rng(25)
     A = O.polar_test_matrix(rng, shape[0], dt) if shape[0] == shape[1] else O.gaussian(rng, *shape, dt)
     info = {}

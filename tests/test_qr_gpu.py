@@ -194,7 +194,7 @@ def test_qr_compact_mixed_parity(mak, cuda, dt, shape):
     Qh, Rh = to_host(Q), to_host(R)
     Qo, Ro = O.qr_compact(A)
     assert O.rel_err(Rh, Ro) <= 1e-12
-    assert O.qr_residual(A, Qh, Rh) <= 5e-13  # BASELINE bound 1e-12
+    assert O.qr_residual(A, Qh, Rh) <= 5e-13  # within the 1e-12 accuracy bound
     # isometry in the reference's relative form (is_left_isometric,
     # src/common/matrixproperties.jl:49-54): ||Q^H Q - I|| <= rtol ||Q^H Q||
     assert O.orth_error(Qh) <= 1e-13 * np.sqrt(Qh.shape[1])
