@@ -113,6 +113,24 @@ def world():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(dist, value, device="cpu"):
+    """The largest of the ranks' values (the whole job takes as long as its
+    slowest replica); `value` itself with one rank."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_tflops(world_size, flops_per_replica, ms):
+    """Whole-job throughput of `world_size` replicas that each factor one
+    matrix of `flops_per_replica` flops, the slowest taking `ms`."""
+    return world_size * flops_per_replica / (ms / 1e3) / 1e12
+
+
 # ------------------------------------------------------------- clocks ---
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons (200 ms)."""
@@ -313,11 +331,7 @@ def measure_qr(mak, lib, args, dev, dist, A_master, precision, steps, warmup, cl
     lib.mak_profile_stop()
     clk = clocks.stop() if clocks is not None else None
     launches = int(lib.mak_kernel_launches() - launches0)
-    ms = e0.elapsed_time(e1) / steps
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(dist, e0.elapsed_time(e1) / steps, dev)
     prof = {name: _read_prof(lib, kid) for name, kid in
             (("gemm_native", 0), ("gemm_split_tensor", 1), ("qr_panel", 2))}
     acc = {"qr_residual": None, "orth_abs_fro": None, "orth_rel": None,
@@ -364,7 +378,7 @@ def run_gb300(args):
     r = measure_qr(mak, lib, args, dev, dist, A_master, args.precision, args.steps, args.warmup,
                    clocks)
     ms = r["ms"]
-    value = ws * flops / (ms / 1e3) / 1e12
+    value = job_tflops(ws, flops, ms)
 
     # dominant kernel class, timed live (CUDA events on its own stream) inside
     # the timed region
@@ -451,12 +465,8 @@ def run_gb300(args):
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
-        ems = s0.elapsed_time(s1) / k2
-        if dist is not None:
-            t = torch.tensor([ems], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ems = float(t.item())
-        out["e2e"] = {"value": round(ws * flops / (ems / 1e3) / 1e12, 5), "unit": "TFLOP/s",
+        ems = max_over_ranks(dist, s0.elapsed_time(s1) / k2, dev)
+        out["e2e"] = {"value": round(job_tflops(ws, flops, ems), 5), "unit": "TFLOP/s",
                       "ms_per_step": round(ems, 3), "steps": k2,
                       "h2d_bytes_per_step": int(A.numel() * 8),
                       "d2h_bytes_per_step": int((Q.numel() + R.numel()) * 8)}
