@@ -180,3 +180,32 @@ def test_orth_algorithm_selection(mak):
             right_orth_alg(bad)
     with pytest.raises(ArgumentError):
         left_orth_alg(GB300_HouseholderQR(), positive=False)
+
+
+def test_every_entry_point_refuses_host_tensors(mak):
+    """No CPU fallback: each public factorization, rule and GEMM raises on a
+    host tensor before any work (the product path is the CUDA library only)."""
+    import torch
+
+    A = torch.zeros((6, 4), dtype=torch.float64)
+    W = torch.zeros((4, 6), dtype=torch.float64)
+    calls = [
+        lambda: mak.qr_compact(A), lambda: mak.qr_full(A), lambda: mak.qr_null(A),
+        lambda: mak.lq_compact(W), lambda: mak.lq_full(W), lambda: mak.lq_null(W),
+        lambda: mak.left_polar(A), lambda: mak.right_polar(W),
+        lambda: mak.left_orth(A), lambda: mak.right_orth(W), lambda: mak.left_null(A),
+        lambda: mak.right_null(W), lambda: mak.project_isometric(A),
+        lambda: mak.gemm(A, W),
+        lambda: mak.qr_pullback_(A, A, (A, A[:4]), (None, None)),
+        lambda: mak.left_polar_pullback_(A, A, (A, A[:4, :4]), (None, None)),
+        lambda: mak.right_polar_pullback_(W, W, (W[:, :4], W), (None, None)),
+        lambda: mak.left_polar_pushforward_(A, A, (A, A[:4, :4])),
+        lambda: mak.right_polar_pushforward_(W, W, (W[:, :4], W)),
+        lambda: mak.qr_null_pullback_(A, A, A[:, :2], A[:, :2]),
+        lambda: mak.lq_pullback_(W, W, (W[:, :4], W), (None, None)),
+        lambda: mak.lq_null_pullback_(W, W, W[:2], W[:2]),
+        lambda: mak.batched_qr_compact([A]), lambda: mak.batched_left_polar([A]),
+    ]
+    for call in calls:
+        with pytest.raises(mak.ArgumentError, match="CUDA device"):
+            call()
