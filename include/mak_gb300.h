@@ -67,7 +67,8 @@ typedef struct {
  * src/interface/decompositions.jl:80-86).  pivoted=true is not provided. */
 typedef struct {
   int32_t positive;  /* 1 (reference default): diag(R) made real >= 0        */
-  int32_t blocksize; /* 0: library default panel width; else 1..64           */
+  int32_t blocksize; /* 0: library default panel width (32); else 1..32;
+                        larger values are rejected (-9)                     */
   int32_t precision; /* MAK_PREC_NATIVE or MAK_PREC_MIXED                     */
   int32_t reserved;
 } mak_qr_opts;
@@ -212,9 +213,10 @@ int mak_qr_compact_d_noalloc(int64_t m, int64_t n, double* A, int64_t lda, doubl
  * so callers can run their own contractions with the same precision control
  * (reference: the mul! calls of src/implementations/polar.jl:63,108,163 and
  * src/pullbacks/{qr,polar}.jl, which go to cuBLAS through CUDA.jl).
- * precision = MAK_PREC_MIXED: Float64 data is split into seven 7-bit bf16
- * digit planes and multiplied on the tcgen05 tensor cores with exact fp32
- * group accumulation (Ozaki scheme); alpha/beta must then be real.
+ * precision = MAK_PREC_MIXED: Float64 data is split into eight balanced 7-bit
+ * bf16 digit planes and the 36 plane pairs of significant weight are
+ * multiplied on the tcgen05 tensor cores with exact fp32 group accumulation
+ * (Ozaki scheme); alpha/beta must then be real.
  */
 int mak_gemm_workspace(int dtype, int opA, int opB, int64_t m, int64_t n, int64_t k,
                        int precision, size_t* bytes);

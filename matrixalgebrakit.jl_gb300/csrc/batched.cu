@@ -11,8 +11,11 @@
 //    remaining SMs concurrently;
 //  * the internal streams fork from and join back into the caller's stream
 //    with events, so the whole batch is one stream-ordered unit that a
-//    caller can capture into a CUDA graph (the streams and events are
-//    created on the first call, which must therefore precede any capture);
+//    caller can capture into a CUDA graph.  The streams and events belong
+//    to the calling host thread and the current device (created by that
+//    thread's first batched call on that device, which must therefore
+//    precede any capture there): calls from several threads never share an
+//    event, and a call on another device never uses this device's streams;
 //  * each stream owns a slice of the caller's workspace sized for the
 //    largest block it runs; every block writes its own mak_info record;
 //  * batched polar runs the Newton iteration in its fixed-iteration mode
@@ -30,22 +33,23 @@ constexpr int BATCH_STREAMS = 8;
 struct StreamPool {
   cudaStream_t s[BATCH_STREAMS];
   cudaEvent_t fork, join[BATCH_STREAMS];
-  bool ok = false;
+  int state = 0;  // 0 not created, 1 ready, -1 failed
 };
 
-static StreamPool& pool() {
-  static StreamPool p;
-  static std::once_flag f;
-  std::call_once(f, [] {
+// the calling thread's pool on the current device (nullptr on failure)
+static StreamPool* pool() {
+  static thread_local StreamPool p[kMaxDevices];
+  StreamPool& q = p[current_device()];
+  if (q.state == 0) {
     bool ok = true;
     for (int i = 0; i < BATCH_STREAMS; i++) {
-      ok &= cudaStreamCreateWithFlags(&p.s[i], cudaStreamNonBlocking) == cudaSuccess;
-      ok &= cudaEventCreateWithFlags(&p.join[i], cudaEventDisableTiming) == cudaSuccess;
+      ok &= cudaStreamCreateWithFlags(&q.s[i], cudaStreamNonBlocking) == cudaSuccess;
+      ok &= cudaEventCreateWithFlags(&q.join[i], cudaEventDisableTiming) == cudaSuccess;
     }
-    ok &= cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming) == cudaSuccess;
-    p.ok = ok;
-  });
-  return p;
+    ok &= cudaEventCreateWithFlags(&q.fork, cudaEventDisableTiming) == cudaSuccess;
+    q.state = ok ? 1 : -1;
+  }
+  return q.state == 1 ? &q : nullptr;
 }
 
 enum { BATCH_QR = 0, BATCH_POLAR = 1 };
@@ -149,8 +153,9 @@ static int batched(int kind, const mak_batch_item* items, int nitems, const void
   if (p.total > work_bytes) return -5;
   if (infos == nullptr && nitems > 0) return -6;
   if (nitems == 0) return 0;
-  StreamPool& sp = pool();
-  if (!sp.ok) return MAK_ERR_CUDA;
+  StreamPool* pp = pool();
+  if (pp == nullptr) return MAK_ERR_CUDA;
+  StreamPool& sp = *pp;
   cudaStream_t st = (cudaStream_t)stream;
   MAK_CUDA_TRY(cudaEventRecord(sp.fork, st));
   for (int s = 0; s < BATCH_STREAMS; s++) MAK_CUDA_TRY(cudaStreamWaitEvent(sp.s[s], sp.fork, 0));
@@ -161,20 +166,19 @@ static int batched(int kind, const mak_batch_item* items, int nitems, const void
     return item_flops(kind, items[a]) > item_flops(kind, items[b]);
   });
   int rc_all = 0;
-  set_lookahead(false);  // the batch's streams already overlap the blocks
-  // a quarter of the SMs per split product, so that several blocks'
-  // persistent tensor-core grids and native kernels share the GPU
-  const int budget0 = split_gemm_cta_budget();
-  set_split_gemm_cta_budget(num_sms() / 4);
-  for (int i : order) {
-    const int s = p.owner[i];
-    Arena ar((char*)work + p.off[s], p.ws_stream[s]);
-    int rc = info_reset(sp.s[s], infos + i);
-    if (rc == 0) rc = item_dispatch(kind, items[i], opts, ar, infos + i, sp.s[s]);
-    if (rc != 0 && rc_all == 0) rc_all = rc;
+  {
+    // the batch's streams already overlap the blocks (no look-ahead), and a
+    // quarter of the SMs per split product lets several blocks' persistent
+    // tensor-core grids and native kernels share the GPU
+    ThreadSettingsScope settings(false, num_sms() / 4);
+    for (int i : order) {
+      const int s = p.owner[i];
+      Arena ar((char*)work + p.off[s], p.ws_stream[s]);
+      int rc = info_reset(sp.s[s], infos + i);
+      if (rc == 0) rc = item_dispatch(kind, items[i], opts, ar, infos + i, sp.s[s]);
+      if (rc != 0 && rc_all == 0) rc_all = rc;
+    }
   }
-  set_lookahead(true);
-  set_split_gemm_cta_budget(budget0);
   for (int s = 0; s < BATCH_STREAMS; s++) {
     MAK_CUDA_TRY(cudaEventRecord(sp.join[s], sp.s[s]));
     MAK_CUDA_TRY(cudaStreamWaitEvent(st, sp.join[s], 0));

@@ -46,6 +46,24 @@ int lookahead_ctas();
 int split_gemm_cta_budget();
 void set_split_gemm_cta_budget(int ctas);
 
+// Scoped form of the two thread-local settings above: the previous values
+// come back on every exit path of the scope.
+struct ThreadSettingsScope {
+  bool lookahead_prev;
+  int budget_prev;
+  ThreadSettingsScope(bool lookahead_on, int gemm_budget)
+      : lookahead_prev(lookahead_enabled()), budget_prev(split_gemm_cta_budget()) {
+    set_lookahead(lookahead_on);
+    set_split_gemm_cta_budget(gemm_budget);
+  }
+  ~ThreadSettingsScope() {
+    set_lookahead(lookahead_prev);
+    set_split_gemm_cta_budget(budget_prev);
+  }
+  ThreadSettingsScope(const ThreadSettingsScope&) = delete;
+  ThreadSettingsScope& operator=(const ThreadSettingsScope&) = delete;
+};
+
 // Left polar decomposition by scaled Newton (W m x n, P n x n or nullptr);
 // tol < 0 selects the fixed-iteration, host-sync-free mode.
 template <class T>

@@ -10,6 +10,7 @@
 #include <math.h>
 
 #include <atomic>
+#include <mutex>
 
 #include "../../include/mak_gb300.h"
 
@@ -294,6 +295,32 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, in
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Host state that is set up lazily (device attributes, kernel attributes,
+// streams, events) belongs to ONE device: a process may drive several GPUs
+// (one per Julia task or host thread), and a kernel attribute set, or a
+// stream created, while device 0 was current does not carry over to
+// device 1.  Such state is kept per device, indexed by cudaGetDevice() at
+// the call.
+constexpr int kMaxDevices = 64;
+inline int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) d = 0;
+  return d;
+}
+// One value per device, computed once per device by `init` (run with that
+// device current; concurrent first calls on one device wait for it).
+template <class V>
+struct PerDevice {
+  std::once_flag flag[kMaxDevices];
+  V val[kMaxDevices] = {};
+  template <class F>
+  V get(F&& init) {
+    const int d = current_device();
+    std::call_once(flag[d], [&] { val[d] = init(); });
+    return val[d];
+  }
+};
 
 // Bump allocator over the caller's workspace.  With base == nullptr it only
 // measures (used by the *_workspace queries, LAPACK's lwork = -1 pattern).

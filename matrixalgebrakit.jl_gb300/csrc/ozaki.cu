@@ -809,14 +809,16 @@ static size_t oz_smem_bytes() {
   return (size_t)OZ_STAGES * S * (OZ_BM * OZ_BK * 2 + OZ_BN * OZ_BK * 2) + 1024;
 }
 
+// the kernels' dynamic shared-memory limit, raised once per device
 template <int S>
 static void oz_set_attr() {
-  static std::once_flag f;
-  std::call_once(f, [] {
+  static PerDevice<int> pd;
+  pd.get([] {
     cudaFuncSetAttribute(oz_gemm_kernel<S, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)oz_smem_bytes<S>());
     cudaFuncSetAttribute(oz_gemm_kernel<S, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)oz_smem_bytes<S>());
+    return 1;
   });
 }
 

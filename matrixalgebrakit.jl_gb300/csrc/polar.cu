@@ -13,7 +13,7 @@
 //
 // The inverse is an in-place blocked Gauss-Jordan elimination with partial
 // pivoting (gje_inverse): per block column of 32 a cooperative panel kernel
-// (pivot search + row exchange + elimination, two bounded grid barriers per
+// (pivot search + row exchange + elimination, one bounded grid barrier per
 // column, panel rows resident in shared memory), a row-exchange/save kernel
 // for the other columns and one rank-32 GEMM update -- 2n^3 flops in total,
 // the same count as the reference's LU + inverse.  The Newton update reads
@@ -252,21 +252,22 @@ __global__ void gje_perm_kernel(int n, const int* piv, int* iperm, const int* sk
   for (int i = threadIdx.x; i < n; i += blockDim.x) iperm[perm[i]] = i;
 }
 
+// slab capacity of the panel kernel; the kernels' dynamic shared-memory
+// limits are raised once per type and device
 template <class T>
 static size_t gj_slab_cap() {
-  static size_t cap = 0;
-  static std::once_flag f;
-  std::call_once(f, [] {
+  static PerDevice<size_t> pd;
+  return pd.get([] {
     cudaFuncAttributes fa;
     size_t stat = 16 * 1024;
     if (cudaFuncGetAttributes(&fa, gje_panel_kernel<T>) == cudaSuccess) stat = fa.sharedSizeBytes;
-    cap = (size_t)max_smem_optin() - stat - 1024;
+    const size_t cap = (size_t)max_smem_optin() - stat - 1024;
     cudaFuncSetAttribute(gje_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)cap);
     cudaFuncSetAttribute(gje_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          max_smem_optin() - 1024);
+    return cap;
   });
-  return cap;
 }
 
 template <class T>

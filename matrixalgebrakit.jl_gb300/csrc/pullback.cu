@@ -29,14 +29,20 @@
 namespace mak {
 
 // ---------------------------------------------------------------- helpers --
-// eps(x)^(3/4) of Julia (`eps(x)` = spacing of floats at x)
+// eps(x)^(3/4) of Julia (`eps(x)` = spacing of floats at x; at 0 and in the
+// subnormal range that spacing is the smallest subnormal, so the tolerance
+// stays positive and an all-zero R has rank 0, as in the reference)
 template <class R>
 __device__ __forceinline__ R eps34(R x) {
-  if (!(x > R(0))) return R(0);
-  int e;
-  frexp(x, &e);  // x = f 2^e, f in [0.5, 1)
   const int mant = sizeof(R) == 8 ? 52 : 23;
-  const R sp = ldexp(R(1), e - 1 - mant);
+  const R tiny = ldexp(R(1), sizeof(R) == 8 ? -1074 : -149);  // smallest subnormal
+  R sp = tiny;
+  if (x > R(0)) {
+    int e;
+    frexp(x, &e);  // x = f 2^e, f in [0.5, 1)
+    const R s = ldexp(R(1), e - 1 - mant);
+    sp = s > tiny ? s : tiny;
+  }
   return pow(sp, R(0.75));
 }
 

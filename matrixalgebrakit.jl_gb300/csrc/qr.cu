@@ -567,23 +567,26 @@ int split_gemm_cta_budget() { return tl_gemm_budget; }
 void set_split_gemm_cta_budget(int ctas) { tl_gemm_budget = ctas > 0 ? ctas : 0; }
 
 // Side stream (highest priority, so its panel CTAs are scheduled ahead of
-// the trailing GEMM's) and events of the look-ahead, one set per host
-// thread so that calls from several threads never share an event; created
-// on the thread's first large call (which must precede any graph capture on
-// that thread).
+// the trailing GEMM's) and events of the look-ahead, one set per (host
+// thread, device) so that calls from several threads never share an event
+// and a call on another device never queues work on this device's stream;
+// created by the first large call of that thread on that device (which must
+// precede any graph capture there).
 LookAhead* lookahead() {
-  static thread_local LookAhead la;
-  static thread_local int state = 0;  // 0 not created, 1 ready, -1 failed
-  if (state == 0) {
+  static thread_local LookAhead la[kMaxDevices];
+  static thread_local int state[kMaxDevices] = {};  // 0 not created, 1 ready, -1 failed
+  const int d = current_device();
+  if (state[d] == 0) {
     int lo = 0, hi = 0;
     cudaDeviceGetStreamPriorityRange(&lo, &hi);
-    state = (cudaStreamCreateWithPriority(&la.side, cudaStreamNonBlocking, hi) == cudaSuccess &&
-             cudaEventCreateWithFlags(&la.ev_ready, cudaEventDisableTiming) == cudaSuccess &&
-             cudaEventCreateWithFlags(&la.ev_done, cudaEventDisableTiming) == cudaSuccess)
-                ? 1
-                : -1;
+    state[d] =
+        (cudaStreamCreateWithPriority(&la[d].side, cudaStreamNonBlocking, hi) == cudaSuccess &&
+         cudaEventCreateWithFlags(&la[d].ev_ready, cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&la[d].ev_done, cudaEventDisableTiming) == cudaSuccess)
+            ? 1
+            : -1;
   }
-  return state == 1 ? &la : nullptr;
+  return state[d] == 1 ? &la[d] : nullptr;
 }
 
 // T factor of a JB-wide block reflector (LAPACK larft, forward, column-wise
@@ -687,43 +690,37 @@ std::atomic<unsigned long long>& launch_counter() {
 }
 
 int num_sms() {
-  static int v = 0;
-  static std::once_flag f;
-  std::call_once(f, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    if (v <= 0) v = 152;
+  static PerDevice<int> pd;
+  return pd.get([] {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, current_device());
+    return v > 0 ? v : 152;
   });
-  return v;
 }
 int max_smem_optin() {
-  static int v = 0;
-  static std::once_flag f;
-  std::call_once(f, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (v <= 0) v = 227 * 1024;
+  static PerDevice<int> pd;
+  return pd.get([] {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, current_device());
+    return v > 0 ? v : 227 * 1024;
   });
-  return v;
 }
 
 // Shared memory available to the panel slab: the opt-in maximum minus the
-// kernel's static shared memory (T-factor scratch), queried once per type.
+// kernel's static shared memory (T-factor scratch); queried, and the
+// kernel's dynamic shared-memory limit raised, once per type and device.
 template <class T>
 static size_t panel_slab_cap() {
-  static size_t cap = 0;
-  static std::once_flag f;
-  std::call_once(f, [] {
+  static PerDevice<size_t> pd;
+  return pd.get([] {
     cudaFuncAttributes fa;
     size_t stat = 48 * 1024;
     if (cudaFuncGetAttributes(&fa, qr_panel_kernel<T>) == cudaSuccess) stat = fa.sharedSizeBytes;
-    cap = (size_t)max_smem_optin() - stat - 1024;
+    const size_t cap = (size_t)max_smem_optin() - stat - 1024;
     cudaFuncSetAttribute(qr_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)cap);
+    return cap;
   });
-  return cap;
 }
 
 // Grid shape of the panel kernel: rows per CTA bounded below by 64 (a grid
