@@ -86,9 +86,10 @@ def parse():
     ap.add_argument("--no-pullback", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-tensors", type=int, default=256)
-    ap.add_argument("--workload", choices=["qr", "gemm", "polar"], default="qr",
+    ap.add_argument("--workload", choices=["qr", "gemm", "polar", "batched"], default="qr",
                     help="gemm: time the split-precision product alone on --gemm-shapes; "
-                         "polar: left_polar! alone on --polar-n (profiling runs)")
+                         "polar: left_polar! alone on --polar-n; batched: the batch of "
+                         "uneven blocks alone (profiling runs)")
     ap.add_argument("--gemm-shapes", type=str, default="16384x8192x128,128x8192x16384",
                     help="MxNxK list for --workload gemm (the trailing-update shapes of the "
                          "16384 x 8192 QR: C -= V W2 and W = V^H C)")
@@ -242,6 +243,126 @@ def cpu_qr_rate(m, n, reps=1):
     return qr_flops(m, n) / t / 1e12, t, cores
 
 
+def _host_info():
+    """CPU model, usable cores and the BLAS library behind scipy's LAPACK."""
+    info = {"cores": len(os.sched_getaffinity(0))}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() in ("Model name", "Architecture", "Socket(s)", "Vendor ID"):
+                info[k.strip().lower().replace(" ", "_").replace("(s)", "s")] = v.strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        import scipy
+
+        cfg = scipy.show_config(mode="dicts")
+        b = cfg["Build Dependencies"]["lapack"]
+        info["blas"] = f"{b.get('name')} {b.get('version')} (scipy {scipy.__version__})"
+    except Exception:  # noqa: BLE001 -- informational only
+        info["blas"] = "scipy-bundled OpenBLAS"
+    info["blas_threads"] = _blas_threads.describe()
+    return info
+
+
+_ONE_THREAD_SNIPPET = r"""
+import json, sys, time
+import numpy as np
+sys.path.insert(0, {root!r})
+import oracle
+import bench
+kind, m, n = {kind!r}, {m}, {n}
+if kind == "qr":
+    A = oracle.gaussian(np.random.default_rng({seed}), m, n, np.float64)
+    oracle.qr_compact(A[:64, :32])
+    t0 = time.perf_counter(); oracle.qr_compact(A); t = time.perf_counter() - t0
+    print(json.dumps({{"s": t, "tflops": bench.qr_flops(m, n) / t / 1e12}}))
+else:
+    A = bench.polar_matrix(n)
+    oracle.left_polar_svd(A[:64, :64])
+    t0 = time.perf_counter(); oracle.left_polar_svd(A); t = time.perf_counter() - t0
+    print(json.dumps({{"s": t}}))
+"""
+
+
+def _one_thread(kind, m, n):
+    """The oracle on one host thread (a child process with OpenBLAS limited to
+    one thread before it loads)."""
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1",
+               MKL_NUM_THREADS="1")
+    code = _ONE_THREAD_SNIPPET.format(root=str(ROOT), kind=kind, m=m, n=n, seed=SEED + 1)
+    try:
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                           timeout=600, cwd=str(ROOT))
+        return json.loads(r.stdout.strip().splitlines()[-1])
+    except (OSError, subprocess.SubprocessError, ValueError, IndexError) as e:
+        return {"error": str(e)[:200]}
+
+
+def host_legs(args, A_np, R_mixed, R_native):
+    """The host-side legs of the benchmark (rank 0, after every GPU timing):
+
+    * parity at the full size: R of the oracle (the reference's
+      LAPACK_HouseholderQR restated) of the same 16384 x 8192 matrix against
+      the GPU's R in both precisions;
+    * the reference's PolarNewton on the host on the same polar matrix: its
+      iteration count k_ref fixes the polar flop count, and its time is the
+      CPU rate of that algorithm;
+    * the CPU baseline: the reference's LAPACK_HouseholderQR and default
+      PolarViaSVD(SafeDivideAndConquer) (?gesdd, ?gesvd fallback) on all host
+      cores over bounded samples, and on one thread over smaller ones."""
+    import numpy as np
+
+    import oracle
+
+    res = {"host": _host_info()}
+    cores = res["host"]["cores"]
+    with _blas_threads(cores):
+        t0 = time.perf_counter()
+        R_ref = oracle.qr_r(A_np)
+        t_r = time.perf_counter() - t0
+        res["r_vs_oracle"] = {"size": f"{A_np.shape[0]}x{A_np.shape[1]}",
+                              "mixed": oracle.rel_err(R_mixed, R_ref) if R_mixed is not None
+                              else None,
+                              "native": oracle.rel_err(R_native, R_ref) if R_native is not None
+                              else None,
+                              "oracle_geqrt_s": round(t_r, 2)}
+        del R_ref
+        if not args.no_polar:
+            P_np = polar_matrix(args.polar_n)
+            t0 = time.perf_counter()
+            _, _, pinfo = oracle.left_polar_newton(P_np, compute_p=True)
+            t_n = time.perf_counter() - t0
+            k_ref = int(pinfo["iterations"])
+            res["polar_newton_oracle"] = {
+                "k_ref": k_ref, "converged": bool(pinfo["converged"]), "s": round(t_n, 2),
+                "tflops": round(polar_flops(args.polar_n, args.polar_n, k_ref) / t_n / 1e12, 5),
+                "what": f"reference PolarNewton on the host, {args.polar_n}^2, all cores"}
+            del P_np
+        ms_, ns_ = (int(x) for x in args.cpu_sample.split("x"))
+        rate, t, _ = cpu_qr_rate(ms_, ns_)
+        res["qr"] = {"value": round(rate, 5), "unit": "TFLOP/s", "threads": cores,
+                     "sample": f"qr_compact positive=true {ms_}x{ns_} Float64 (LAPACK ?geqrt "
+                               f"nb=36 + ?gemqrt + gaugefix)", "s": round(t, 3)}
+        ps = max(256, min(args.polar_n, 2048))
+        P_s = polar_matrix(ps)
+        oracle.left_polar_svd(P_s[:256, :256])
+        t0 = time.perf_counter()
+        oracle.left_polar_svd(P_s)
+        t_svd = time.perf_counter() - t0
+        res["polar"] = {"s": round(t_svd, 3), "threads": cores,
+                        "factorizations_per_s": round(1.0 / t_svd, 4),
+                        "sample": f"left_polar! PolarViaSVD(SafeDivideAndConquer) (?gesdd, "
+                                  f"?gesvd fallback, gaugefix) on the {ps}x{ps} polar matrix"}
+        del P_s
+    q1 = _one_thread("qr", 2048, 1024)
+    p1 = _one_thread("polar", 1024, 1024)
+    res["threads_1"] = {"qr": {"sample": "qr_compact 2048x1024 Float64", **q1},
+                        "polar": {"sample": "PolarViaSVD 1024x1024 polar matrix", **p1}}
+    return res
+
+
 def run_reference(args):
     rank, ws, _ = world()
     if rank != 0:
@@ -272,7 +393,8 @@ def run_reference(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic iid N(0,1), seeded",
         "config": config_of(args),
         "cpu_baseline": {"value": round(val, 5), "unit": "TFLOP/s", "cores": cores,
-                         "kind": "port", "sample": sample, "blas": blas},
+                         "kind": "port", "sample": sample, "blas": blas,
+                         "threads_all": cores, "host": _host_info()},
         "e2e": {"value": round(val, 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "accuracy": {"qr_residual": oracle.qr_residual(A, Q, R)},
@@ -286,7 +408,9 @@ def config_of(args):
                         f"iid N(0,1)", "m": args.m, "n": args.n, "precision": args.precision,
             "parallelism": f"replicas x{args.gpus}",
             "l2": "inputs larger than L2 (A is %.2f GB > 129 MB L2), no flush needed"
-                  % (args.m * args.n * 8 / 1e9)}
+                  % (args.m * args.n * 8 / 1e9),
+            "cpu_sample": f"host CPU legs (cpu_baseline, --impl reference) time a bounded "
+                          f"{args.cpu_sample} sample of the same distribution per step"}
 
 
 # ------------------------------------------------------------ GB300 arm ---
@@ -425,6 +549,8 @@ def run_gb300(args):
                           if p_ms > 0 else None},
                 "breakdown": breakdown}
 
+    want_host = rank == 0 and not args.no_cpu_baseline and not args.lean
+    R_mixed_h = r["R"].cpu().numpy() if want_host else None
     out = {
         "metric": METRIC, "value": round(value, 5), "unit": "TFLOP/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -474,8 +600,11 @@ def run_gb300(args):
     del r
 
     # the plain FP64 kernels on the same input: the comparison the metric asks for
+    R_native_h = None
     if mixed and not args.lean and args.fp64_steps > 0:
         r64 = measure_qr(mak, lib, args, dev, dist, A_master, "native", args.fp64_steps, 1)
+        if want_host:
+            R_native_h = r64["R"].cpu().numpy()
         v64 = ws * flops / (r64["ms"] / 1e3) / 1e12
         out["fp64"] = {"value": round(v64, 5), "unit": "TFLOP/s",
                        "ms_per_step": round(r64["ms"], 3), "steps": args.fp64_steps,
@@ -499,14 +628,31 @@ def run_gb300(args):
     if not args.no_sweep and not args.lean:
         out["orth_sweep"] = sweep_measure(mak, args, dev)
 
-    if rank == 0 and not args.no_cpu_baseline and not args.lean:
-        ms_, ns_ = (int(x) for x in args.cpu_sample.split("x"))
-        rate, t, cores = cpu_qr_rate(ms_, ns_)
-        out["cpu_baseline"] = {"value": round(rate, 5), "unit": "TFLOP/s", "cores": cores,
-                               "kind": "port",
-                               "sample": f"one qr_compact positive=true {ms_}x{ns_} Float64 "
-                                         f"(LAPACK ?geqrt nb=36 + ?gemqrt + gaugefix), "
-                                         f"{t:.2f} s"}
+    if want_host:
+        del A_master
+        torch.cuda.empty_cache()
+        h = host_legs(args, A_host.numpy(), R_mixed_h, R_native_h)
+        del R_mixed_h, R_native_h
+        out["accuracy"]["r_vs_oracle"] = h["r_vs_oracle"]
+        po = h.get("polar_newton_oracle")
+        if po and "polar" in out:
+            # credit the reference's iteration count, not this run's own
+            for key in ("polar", "polar_fp64"):
+                if key in out:
+                    pm = out[key]
+                    pm["k_ref"] = po["k_ref"]
+                    pm["tflops"] = round(polar_flops(args.polar_n, args.polar_n, po["k_ref"]) /
+                                         (pm["ms"] / 1e3) / 1e12, 4)
+                    pm["flop_count"] = ("k_ref*8n^3/3 + 2n^3: the reference PolarNewton count "
+                                        "with the oracle's iteration count on the same matrix "
+                                        "(Newton-Schulz steps not credited)")
+        qr_ = h["qr"]
+        out["cpu_baseline"] = {
+            "value": qr_["value"], "unit": "TFLOP/s", "cores": h["host"]["cores"], "kind": "port",
+            "sample": f"{qr_['sample']}, {qr_['s']:.2f} s per factorization, all cores",
+            "qr": qr_, "polar": h["polar"], "polar_newton": po,
+            "threads_all": h["host"]["cores"], "threads_1": h["threads_1"],
+            "host": h["host"]}
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
@@ -606,22 +752,43 @@ def batched_measure(mak, args, dev):
     # polar (batched: up to 10 Newton iterations, each block stopped on the
     # device at the default tolerance) in both precisions
     for prec in ("native", "mixed"):
-        def run_polar(iters=None):
+        def restore():
             for w, s_ in zip(work, srcs):
                 w.copy_(s_)
+
+        def run_polar(iters=None, outs=None):
+            restore()
             return mak.batched_left_polar(work, copy_inputs=False, precision=prec, maxiter=10,
-                                          _info=iters)
+                                          outs=outs, _info=iters)
 
         iters = []
-        outs = run_polar(iters)
-        ms = timed(run_polar, reps=1)
+        outs = run_polar(iters)  # eager: also creates the internal streams
+        ms_eager = timed(lambda: run_polar(outs=outs), reps=1)
+        # the whole batch (inputs restored inside the graph) as one CUDA graph
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            restore()
+            with torch.cuda.graph(g, stream=s):
+                restore()
+                mak.batched_left_polar(work, copy_inputs=False, outs=outs, precision=prec,
+                                       maxiter=10, _capturing=True)
+        torch.cuda.current_stream().wait_stream(s)
+        ms = timed(g.replay)
         back = max(float(torch.linalg.norm(s_ - W @ P) / torch.linalg.norm(s_))
-                   for s_, (W, P) in zip(srcs[:8] + srcs[-8:], outs[:8] + outs[-8:]))
-        res[f"polar_{prec}"] = {"ms": round(ms, 3), "blocks_per_s": round(nb * 1e3 / ms, 1),
+                   for s_, (W, P) in zip(srcs, outs))
+        res[f"polar_{prec}"] = {"graph_ms": round(ms, 3), "eager_ms": round(ms_eager, 3),
+                                "blocks_per_s": round(nb * 1e3 / ms, 1),
                                 "newton_iterations_max": max(iters) if iters else None,
                                 "newton_iterations_mean": round(sum(iters) / len(iters), 2)
                                 if iters else None, "maxiter": 10,
-                                "max_back_err_sampled": back}
+                                "max_back_err": back}
+        del g
+    for kind in ("qr", "polar"):
+        a = res[f"{kind}_native"]["graph_ms"]
+        b = res[f"{kind}_mixed"]["graph_ms"]
+        res[f"{kind}_mixed_over_native"] = round(a / b, 3)
     return res
 
 
@@ -716,11 +883,11 @@ def sweep_measure(mak, args, dev):
     return res
 
 
-def polar_measure(mak, args, dev, precision):
+def polar_matrix(n):
+    """The single large polar problem: A = U diag(s) V^T with U, V Haar
+    (QR of a Gaussian with the sign fix) and s log-spaced from 1 to 1e-6."""
     import numpy as np
-    import torch
 
-    n = args.polar_n
     rng = np.random.default_rng(SEED + 7)
 
     def haar(k):
@@ -730,8 +897,16 @@ def polar_measure(mak, args, dev, precision):
 
     U, V = haar(n), haar(n)
     s = np.logspace(0, -6, n)
-    A_np = (U * s[None, :]) @ V.T
-    A0 = torch.from_numpy(np.asfortranarray(A_np)).to(dev)
+    return np.asfortranarray((U * s[None, :]) @ V.T)
+
+
+def polar_measure(mak, args, dev, precision):
+    import numpy as np
+    import torch
+
+    n = args.polar_n
+    A_np = polar_matrix(n)
+    A0 = torch.from_numpy(A_np).to(dev)
     A = torch.empty_like(A0)
     W, P = mak.polar.initialize_output(A0)
     alg = mak.GB300_PolarNewton(precision=precision)
@@ -753,7 +928,8 @@ def polar_measure(mak, args, dev, precision):
     return {"workload": f"left_polar! PolarNewton, {n}x{n} Float64, U diag(logspace(0,-6)) V^T",
             "precision": precision, "ms": round(ms, 2), "iterations": k,
             "tflops": round(polar_flops(n, n, k) / (ms / 1e3) / 1e12, 4),
-            "flop_count": "k*8n^3/3 + 2n^3 (reference PolarNewton count with its own k)",
+            "flop_count": "k*8n^3/3 + 2n^3 with this run's own k (replaced by the oracle's "
+                          "k_ref when the host legs run)",
             "back_err": back, "orth_abs_fro": orth, "orth_rel": orth / math.sqrt(n),
             "steps": 1, "warmup": 1}
 
@@ -835,12 +1011,28 @@ def run_polar_only(args):
     return 0
 
 
+def run_batched_only(args):
+    """The batch of uneven blocks alone (both precisions, QR and polar): the
+    case the batched kernels are profiled on."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    mak = ge.load_package()
+    print(json.dumps(batched_measure(mak, args, dev)), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "gemm":
         return run_gemm(args)
+    if args.workload == "batched":
+        return run_batched_only(args)
     if args.workload == "polar":
         return run_polar_only(args)
     return run_gb300(args)

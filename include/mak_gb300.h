@@ -111,6 +111,17 @@ int mak_profile_start(void);
 int mak_profile_stop(void);
 int mak_profile_read(int kind, double* total_ms, double* total_work, uint64_t* launches);
 
+/* Self-test of the failure path of the bounded device-side waits (no
+ * counterpart in the reference, whose waits are inside LAPACK / CUSOLVER).
+ * Launches `ctas` co-resident CTAs that meet at the grid barrier the panel
+ * kernels use, expecting ctas + `missing` arrivals, each CTA polling at most
+ * `spin_limit` times (1 .. 2^22).  With missing > 0 the wait gives up and
+ * the DEVICE int *status becomes MAK_ERR_TIMEOUT; with missing = 0 it stays
+ * 0.  `work` is a device buffer of at least 8 bytes.  The kernel always
+ * returns and the context stays usable. */
+int mak_selftest_barrier(int ctas, int missing, int64_t spin_limit, void* work,
+                         size_t work_bytes, int* status, mak_stream_t stream);
+
 /* ------------------------------------------------------------------- QR ---
  * qr_compact!(A, (Q, R), GB300_HouseholderQR(; positive, blocksize))
  * Replaces the reference's qr_householder! (src/implementations/qr.jl:132-188:

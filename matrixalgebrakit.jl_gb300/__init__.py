@@ -63,3 +63,7 @@ __all__ += ["RightOrthViaLQ", "RightOrthViaPolar", "left_orth", "left_orth_", "r
             "right_orth_", "left_null", "left_null_", "right_null", "right_null_",
             "project_isometric", "project_isometric_", "left_orth_alg", "right_orth_alg",
             "batched_left_orth", "batched_project_isometric"]
+
+from . import autodiff  # noqa: E402  (torch.autograd front-end over the device pullbacks)
+
+__all__ += ["autodiff"]

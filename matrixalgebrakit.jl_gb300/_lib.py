@@ -124,6 +124,8 @@ for _s in "dzsc":
     SIGNATURES[f"mak_lq_pullback_{_s}"] = SIGNATURES[f"mak_qr_pullback_{_s}"]
 SIGNATURES["mak_right_polar_pushforward_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
                                                                  C.POINTER(_sz)])
+# self-test of the bounded device waits (failure path)
+SIGNATURES["mak_selftest_barrier"] = (C.c_int, [C.c_int, C.c_int, _i64, _p, _sz, _p, _p])
 
 _lib = None
 _load_error = None

@@ -250,7 +250,8 @@ __device__ __forceinline__ R block_max(R v, R* sh) {
 // never hang the GPU.  `bar[0]` counts arrivals, `bar[1]` is the generation.
 constexpr long long kSpinLimit = 1ll << 22;  // x >=64 ns sleep -> well under a minute
 
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status,
+                                             long long spin_limit = kSpinLimit) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -267,7 +268,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, in
       } else {
         long long spins = 0;
         while (*vgen == g) {
-          if (++spins > kSpinLimit) { atomicExch(status, MAK_ERR_TIMEOUT); ok = 0; break; }
+          if (++spins > spin_limit) { atomicExch(status, MAK_ERR_TIMEOUT); ok = 0; break; }
           if (*((volatile int*)status) == MAK_ERR_TIMEOUT) { ok = 0; break; }
           __nanosleep(64);
         }
@@ -279,6 +280,30 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, in
   __syncthreads();
   return ok_s != 0;
 }
+
+// Barrier of the CTAs that factor one panel together.  SYNC_GRID: the
+// bounded global barrier above, inside a cooperative launch (any number of
+// co-resident CTAs).  SYNC_CLUSTER: the hardware barrier of a thread-block
+// cluster (all of the panel's CTAs form one cluster of at most 8): its
+// arrive.release / wait.acquire pair orders every write of the CTAs (global
+// memory included) before the reads that follow it in the other CTAs, with
+// no polling of global memory.  It needs no bound: the kernels that use it
+// take the same branches in every CTA, so every thread of the cluster
+// arrives.  Unlike a cooperative launch, cluster launches of different
+// streams run side by side.
+enum { SYNC_GRID = 0, SYNC_CLUSTER = 1 };
+template <int SYNC>
+__device__ __forceinline__ bool panel_sync(unsigned* bar, unsigned nblocks, int* status) {
+  if constexpr (SYNC == SYNC_CLUSTER) {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                     : "memory");
+    return true;
+  } else {
+    return grid_barrier(bar, nblocks, status);
+  }
+}
+// largest cluster the panels use (the portable limit)
+constexpr int kPanelClusterMax = 8;
 
 // --------------------------------------------------------------- host side --
 #define MAK_CUDA_TRY(expr)                         \

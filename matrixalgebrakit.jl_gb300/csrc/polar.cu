@@ -12,9 +12,11 @@
 //   W = Q X  (m > n)  or  W = X,     P = herm(W^H A)
 //
 // The inverse is an in-place blocked Gauss-Jordan elimination with partial
-// pivoting (gje_inverse): per block column of 32 a cooperative panel kernel
-// (pivot search + row exchange + elimination, one bounded grid barrier per
-// column, panel rows resident in shared memory), a row-exchange/save kernel
+// pivoting (gje_inverse): per block column of 32 a panel kernel (pivot
+// search + row exchange + elimination, one barrier per column, panel rows
+// resident in shared memory; a thread-block cluster of up to 8 CTAs for
+// n <= 2048, a cooperative grid with a bounded global barrier beyond), a
+// row-exchange/save kernel
 // for the other columns and one rank-32 GEMM update -- 2n^3 flops in total,
 // the same count as the reference's LU + inverse.  The Newton update reads
 // X^{-H} straight out of the eliminated matrix through the inverse column
@@ -34,6 +36,7 @@ namespace mak {
 constexpr int GJ_NB = 32;
 constexpr int GJ_OUTER_NB = 128;  // block column of the mixed-precision path
 constexpr int GJ_THREADS = 256;
+constexpr int GJ_CLUSTER_ROWS = 256;  // rows per CTA up to which a panel runs as one cluster
 
 template <class T>
 struct GjArgs {
@@ -62,7 +65,7 @@ __device__ __forceinline__ void amax_merge(R& v, int& i, R v2, int i2) {
   if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
 }
 
-template <class T>
+template <class T, int SYNC>
 __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
   using R = real_t<T>;
   if (skipped(a.skip)) return;  // the same in every CTA: no barrier is reached
@@ -139,7 +142,7 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
         for (int c = tid; c < b; c += blockDim.x)
           cand[(int64_t)cb * GJ_NB + c] = Ps[(li - r0) + c * rpc];
     }
-    if (!grid_barrier(a.bar, G, a.status)) return;
+    if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
 
     // ---- global pivot (identical in every CTA), then the exchange
     if (wid == 0) {
@@ -260,10 +263,13 @@ static size_t gj_slab_cap() {
   return pd.get([] {
     cudaFuncAttributes fa;
     size_t stat = 16 * 1024;
-    if (cudaFuncGetAttributes(&fa, gje_panel_kernel<T>) == cudaSuccess) stat = fa.sharedSizeBytes;
+    if (cudaFuncGetAttributes(&fa, gje_panel_kernel<T, SYNC_GRID>) == cudaSuccess)
+      stat = fa.sharedSizeBytes;
     const size_t cap = (size_t)max_smem_optin() - stat - 1024;
-    cudaFuncSetAttribute(gje_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)cap);
+    cudaFuncSetAttribute(gje_panel_kernel<T, SYNC_GRID>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+    cudaFuncSetAttribute(gje_panel_kernel<T, SYNC_CLUSTER>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
     cudaFuncSetAttribute(gje_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          max_smem_optin() - 1024);
     return cap;
@@ -318,6 +324,40 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
   // one 32-wide panel (cooperative launch, at most max_ctas CTAs: on the
   // look-ahead side stream it leaves the other SMs to the main stream)
   auto panel = [&](int64_t k0, int b, cudaStream_t s, int max_ctas) -> int {
+    GjArgs<T> ga{X, ldx, (int)n, (int)k0, b, 0, piv, part_val, part_idx, swapbuf,
+                 cand, sms, bar, &info->status, &info->singular, skip_flag()};
+    // n <= 8 x 256: one thread-block cluster of at most 8 CTAs (>= 64 rows
+    // each); clusters of different streams run side by side
+    if (n <= (int64_t)kPanelClusterMax * GJ_CLUSTER_ROWS &&
+        (size_t)GJ_CLUSTER_ROWS * (b + 1) * sizeof(T) <= cap) {
+      int64_t G = ceil_div(n, 64);
+      if (G > kPanelClusterMax) G = kPanelClusterMax;
+      const int64_t rpc = ceil_div(n, G);
+      G = ceil_div(n, rpc);
+      ga.rpc = (int)rpc;
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute attr[1];
+      cfg.gridDim = dim3((unsigned)G);
+      cfg.blockDim = dim3(GJ_THREADS);
+      cfg.dynamicSmemBytes = (size_t)rpc * (b + 1) * sizeof(T);
+      cfg.stream = s;
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)G;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, gje_panel_kernel<T, SYNC_CLUSTER>, &cfg) ==
+              cudaSuccess &&
+          nclusters >= 1) {
+        ProfScope prof(s, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
+        note_launch();
+        MAK_CUDA_TRY(cudaLaunchKernelEx(&cfg, gje_panel_kernel<T, SYNC_CLUSTER>, ga));
+        return 0;
+      }
+      (void)cudaGetLastError();  // fall through to the cooperative grid
+    }
     // grid: rows per CTA >= 64, at most one CTA per SM, slab within shared memory
     int64_t G = ceil_div(n, 64);
     if (G > max_ctas) G = max_ctas;
@@ -331,17 +371,16 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
     G = ceil_div(n, rpc);
     size_t smem = (size_t)rpc * (b + 1) * sizeof(T);
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_kernel<T>, GJ_THREADS,
-                                                      smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_kernel<T, SYNC_GRID>,
+                                                      GJ_THREADS, smem) != cudaSuccess ||
         (int64_t)per_sm * sms < G)
       return MAK_ERR_UNSUPPORTED;
-    GjArgs<T> ga{X, ldx, (int)n, (int)k0, b, (int)rpc, piv, part_val, part_idx, swapbuf,
-                 cand, sms, bar, &info->status, &info->singular, skip_flag()};
+    ga.rpc = (int)rpc;
     void* args[] = {&ga};
     ProfScope prof(s, PROF_GJ_PANEL, 2.0 * (double)n * b * sizeof(T));
     note_launch();
-    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)gje_panel_kernel<T>, dim3((unsigned)G),
-                                             dim3(GJ_THREADS), args, smem, s));
+    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)gje_panel_kernel<T, SYNC_GRID>,
+                                             dim3((unsigned)G), dim3(GJ_THREADS), args, smem, s));
     return 0;
   };
   // the panels of block column [K0, K0 + KB) with their updates confined to

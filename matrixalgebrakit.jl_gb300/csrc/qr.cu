@@ -9,9 +9,13 @@
 //     src/common/safemethods.jl:10-11)
 //
 // Structure on the device, per panel of jb <= 32 columns starting at j0:
-//  1. qr_panel_kernel: ONE cooperative launch factors the (m-j0) x jb panel.
+//  1. qr_panel_kernel: ONE launch factors the (m-j0) x jb panel: a
+//     thread-block cluster of up to 8 CTAs for panels of up to 8 x 256 rows
+//     (hardware cluster barrier; clusters of different streams run side by
+//     side, which the batched driver relies on), a cooperative grid of up to
+//     one CTA per SM beyond that (bounded global barrier).
 //     Each CTA keeps a contiguous slab of panel rows resident in shared
-//     memory for the whole panel; a column costs one bounded grid barrier:
+//     memory for the whole panel; a column costs one barrier:
 //     the reflector norm and the dot products of the still unscaled column
 //     with the columns to its right are published together, and w = v^H A
 //     follows from them once beta/tau are known.  Norms are plain sums of
@@ -196,7 +200,7 @@ __device__ __forceinline__ void larfg_scalars_ssq(T alpha, real_t<T> ssq, real_t
   }
 }
 
-template <class T>
+template <class T, int SYNC>
 __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T> a) {
   using R = real_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -287,7 +291,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
         pn[a.gstride + b] = NK::val(m);
       }
     }
-    if (!grid_barrier(a.bar, G, a.status)) return;
+    if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
 
     // ---- phase B: every CTA combines the partials in the same fixed order
     // and so derives bit-identical beta / tau / w.  Warp 0: the norm; every
@@ -340,7 +344,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
       for (int r = rs + tid; r < nr; r += blockDim.x) ssq_scaled_add(ss2, col[r], scale);
       ss2 = block_sum(ss2, red_r);
       if (tid == 0) a.part_nrm[6 * a.gstride + b] = ss2;
-      if (!grid_barrier(a.bar, G, a.status)) return;
+      if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
       if (wid == 0) {
         R s2 = R(0);
         for (int q = lane; q < G; q += 32) s2 += ld_cg(&a.part_nrm[6 * a.gstride + q]);
@@ -389,7 +393,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
         s = warp_sum(s);
         if (lane == 0) pw2[(int64_t)b * NBMAX + c] = s;
       }
-      if (!grid_barrier(a.bar, G, a.status)) return;
+      if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
       {
         const int per = (G + nw - 1) / nw;
         const int q0 = wid * per, q1 = min(G, q0 + per);
@@ -451,7 +455,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
   }
   for (int c = 0; c < jb; c++)
     for (int r = tid; r < nr; r += blockDim.x) a.A[(r0 + r) + (int64_t)c * a.lda] = Ps[r + c * ldp];
-  if (!grid_barrier(a.bar, G, a.status)) return;
+  if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
 
   // ---- reduce the Gram over the CTAs: one thread per pair, the CTAs'
   // partials in a fixed order (four interleaved accumulators)
@@ -473,7 +477,7 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
     for (; q < G; q++) s0 += ld_cg(src + q * NN);
     a.gram[i + jj * NBMAX] = (s0 + s1) + (s2 + s3);
   }
-  if (!grid_barrier(a.bar, G, a.status)) return;
+  if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
 
   // ---- T factor (larft, forward, column-wise): T = U^{-1} with U_ii =
   // 1/tau_i and U_il = G_il (i < l), each column an independent back
@@ -715,19 +719,29 @@ static size_t panel_slab_cap() {
   return pd.get([] {
     cudaFuncAttributes fa;
     size_t stat = 48 * 1024;
-    if (cudaFuncGetAttributes(&fa, qr_panel_kernel<T>) == cudaSuccess) stat = fa.sharedSizeBytes;
+    if (cudaFuncGetAttributes(&fa, qr_panel_kernel<T, SYNC_GRID>) == cudaSuccess)
+      stat = fa.sharedSizeBytes;
     const size_t cap = (size_t)max_smem_optin() - stat - 1024;
-    cudaFuncSetAttribute(qr_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)cap);
+    cudaFuncSetAttribute(qr_panel_kernel<T, SYNC_GRID>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+    cudaFuncSetAttribute(qr_panel_kernel<T, SYNC_CLUSTER>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
     return cap;
   });
 }
 
-// Grid shape of the panel kernel: rows per CTA bounded below by 64 (a grid
-// barrier is only paid when there is real parallel work) and above by the
-// shared-memory slab size; at most one CTA per SM (cooperative launch).
+// Panels of at most this many rows per CTA (times the cluster limit) run as
+// one thread-block cluster: below it a column's FP64 work per CTA stays
+// smaller than what a global barrier costs.
+constexpr int PANEL_CLUSTER_ROWS = 256;
+
+// Launch shape of the panel kernel.  Cluster (sync = SYNC_CLUSTER): panels
+// of up to kPanelClusterMax x PANEL_CLUSTER_ROWS rows, at least 64 rows per
+// CTA.  Cooperative grid (SYNC_GRID) beyond that: rows per CTA bounded below
+// by 64 (a grid barrier is only paid when there is real parallel work) and
+// above by the shared-memory slab size; at most one CTA per SM.
 struct PanelShape {
-  int G, rpc;
+  int G, rpc, sync;
   size_t smem;
 };
 template <class T>
@@ -735,6 +749,37 @@ static int panel_shape(int64_t mp, int jb, PanelShape& ps, int want_ctas) {
   const int max_ctas = num_sms();
   const size_t cap = panel_slab_cap<T>();
   int64_t rpc_max = (int64_t)(cap / ((size_t)jb * sizeof(T))) - 1;  // ld = rpc | 1
+  const int64_t cl_rows = rpc_max < PANEL_CLUSTER_ROWS ? rpc_max : PANEL_CLUSTER_ROWS;
+  if (mp <= (int64_t)kPanelClusterMax * cl_rows) {
+    int64_t G = ceil_div(mp, 64);
+    if (G > kPanelClusterMax) G = kPanelClusterMax;
+    if (G < 1) G = 1;
+    int64_t rpc = ceil_div(mp, G);
+    if (rpc < 1) rpc = 1;
+    G = ceil_div(mp, rpc);
+    if (G < 1) G = 1;
+    ps.G = (int)G;
+    ps.rpc = (int)rpc;
+    ps.sync = SYNC_CLUSTER;
+    ps.smem = (size_t)(ps.rpc | 1) * jb * sizeof(T);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    cfg.gridDim = dim3((unsigned)G);
+    cfg.blockDim = dim3(PANEL_THREADS);
+    cfg.dynamicSmemBytes = ps.smem;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_kernel<T, SYNC_CLUSTER>, &cfg) ==
+            cudaSuccess &&
+        nclusters >= 1)
+      return 0;
+    (void)cudaGetLastError();  // fall through to the cooperative grid
+  }
   int64_t G = ceil_div(mp, 64);
   if (G > want_ctas) G = want_ctas;
   if (G > max_ctas) G = max_ctas;
@@ -750,10 +795,11 @@ static int panel_shape(int64_t mp, int jb, PanelShape& ps, int want_ctas) {
   if (G < 1) G = 1;
   ps.G = (int)G;
   ps.rpc = (int)rpc;
+  ps.sync = SYNC_GRID;
   ps.smem = (size_t)(ps.rpc | 1) * jb * sizeof(T);
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_panel_kernel<T>, PANEL_THREADS,
-                                                    ps.smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_panel_kernel<T, SYNC_GRID>,
+                                                    PANEL_THREADS, ps.smem) != cudaSuccess)
     return MAK_ERR_CUDA;
   if ((int64_t)per_sm * max_ctas < G) return MAK_ERR_UNSUPPORTED;
   return 0;
@@ -881,10 +927,26 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     PanelArgs<T> pa{A + j0 + j0 * lda, lda, (int)mp, jb, ps.rpc, tau + j0,
                     Ts + (j0 / nb) * NBMAX * NBMAX, part_nrm, part_w, part_g, alpha_buf,
                     gram_buf, bar, status, gmax};
-    void* args[] = {&pa};
     ProfScope prof(s, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
     note_launch();
-    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)qr_panel_kernel<T>, dim3(ps.G),
+    if (ps.sync == SYNC_CLUSTER) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute attr[1];
+      cfg.gridDim = dim3((unsigned)ps.G);
+      cfg.blockDim = dim3(PANEL_THREADS);
+      cfg.dynamicSmemBytes = ps.smem;
+      cfg.stream = s;
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = (unsigned)ps.G;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      MAK_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_kernel<T, SYNC_CLUSTER>, pa));
+      return 0;
+    }
+    void* args[] = {&pa};
+    MAK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)qr_panel_kernel<T, SYNC_GRID>, dim3(ps.G),
                                              dim3(PANEL_THREADS), args, ps.smem, s));
     return 0;
   };

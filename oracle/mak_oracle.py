@@ -16,7 +16,7 @@ from scipy.linalg import lapack
 
 __all__ = [
     "defaulttol", "sign_safe", "default_qr_blocksize",
-    "qr_compact", "qr_full", "qr_null", "project_hermitian", "svd_compact",
+    "qr_compact", "qr_r", "qr_full", "qr_null", "project_hermitian", "svd_compact",
     "left_polar_svd", "left_polar_newton", "qr_rank", "qr_pullback",
     "remove_qr_gauge_dependence", "left_polar_pullback", "sylvester",
     "gaussian", "haar", "polar_test_matrix", "rank_deficient", "batched_blocks",
@@ -129,6 +129,27 @@ def qr_compact(A, positive: bool = True, blocksize: int = 0):
     driver (src/implementations/qr.jl:110-113,132-188): Q is m x min(m,n),
     R is min(m,n) x n."""
     return _qr_householder(A, full=False, positive=positive, blocksize=blocksize)
+
+
+def qr_r(A, positive: bool = True, blocksize: int = 0):
+    """R alone of ``qr_compact!(A, (Q, R))`` with the LAPACK driver: the same
+    ``geqrt`` (nb = min(m, n, 36)), ``uppertriangular!`` copy and the R half
+    of ``gaugefix!`` (src/implementations/qr.jl:132-188,
+    src/common/gauge.jl:16-25) as :func:`qr_compact`, without forming Q
+    (the geqrt call and R's values are identical)."""
+    A = np.array(A, order="F", copy=True)
+    m, n = A.shape
+    k = min(m, n)
+    if k == 0:
+        return np.zeros((k, n), dtype=A.dtype, order="F")
+    nb = blocksize if blocksize > 0 else default_qr_blocksize(m, n)
+    Apk, T, info = _lp("geqrt", A.dtype)(min(k, nb), A)
+    assert info == 0, f"?geqrt info={info}"
+    R = np.asfortranarray(np.triu(Apk[:k, :]))
+    if positive:
+        s = sign_safe(np.diagonal(Apk)[:k].copy())
+        R *= np.conj(s)[:, None]
+    return R
 
 
 def qr_full(A, positive: bool = True, blocksize: int = 0):

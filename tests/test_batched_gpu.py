@@ -97,3 +97,39 @@ def test_batched_polar_stops_on_device(mak, cuda, precision):
         assert O.rel_err(to_host(P), to_host(P1)) <= tol
         assert np.linalg.norm(A - to_host(W) @ to_host(P)) / np.linalg.norm(A) <= 1e-13
         assert O.orth_error(to_host(W)) <= 1e-12
+
+
+def test_batched_two_threads_two_streams(mak, cuda):
+    """Two host threads call the batched QR at the same time, each on its
+    own stream: the internal streams and events belong to the calling thread
+    (and device), so neither call waits on or runs ahead of the other's
+    inputs, and both results equal the oracle's."""
+    import threading
+
+    sets = {"a": _blocks(81, 14, 300), "b": _blocks(82, 14, 300)}
+    results, errors = {}, []
+    gate = threading.Barrier(2)
+
+    def run(name):
+        try:
+            s = torch.cuda.Stream(device=cuda)
+            with torch.cuda.stream(s):
+                devs = [to_dev(A, cuda) for A in sets[name]]
+                gate.wait()
+                for _ in range(3):
+                    outs = mak.batched_qr_compact(devs, precision="mixed")
+                s.synchronize()
+                results[name] = [(to_host(Q), to_host(R)) for Q, R in outs]
+        except Exception as e:  # reported on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=run, args=(k,)) for k in sets]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for name, blocks in sets.items():
+        for A, (Q, R) in zip(blocks, results[name]):
+            assert O.rel_err(R, O.qr_compact(A)[1]) <= 1e-12
+            assert O.qr_residual(A, Q, R) <= 5e-13
