@@ -83,10 +83,15 @@ def parse():
     ap.add_argument("--polar-n", type=int, default=8192)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batched-blocks", type=int, default=300)
+    ap.add_argument("--batched-kinds", type=str, default="qr,polar",
+                    help="which batched factorizations to measure (comma list of qr, polar)")
+    ap.add_argument("--no-batched-loop", action="store_true",
+                    help="skip the per-block launch loop the batched QR is compared with")
     ap.add_argument("--no-pullback", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-tensors", type=int, default=256)
-    ap.add_argument("--workload", choices=["qr", "gemm", "polar", "batched"], default="qr",
+    ap.add_argument("--workload", choices=["qr", "gemm", "polar", "batched", "sweep"],
+                    default="qr",
                     help="gemm: time the split-precision product alone on --gemm-shapes; "
                          "polar: left_polar! alone on --polar-n; batched: the batch of "
                          "uneven blocks alone (profiling runs)")
@@ -564,39 +569,73 @@ def run_gb300(args):
         "clocks": r["clocks"],
     }
 
-    # end-to-end through the public API with host buffers
+    # end-to-end through the public API with host buffers: a stream of
+    # independent factorizations, each step copying its input from pinned
+    # host memory and its factors back.  Two sets of device buffers let the
+    # copies of one step run on the copy engines while the kernels of the
+    # next run on the SMs (H2D and D2H on streams of their own, ordered with
+    # events), as a caller factoring one matrix after another would.
     if not args.no_e2e and not args.lean:
-        A, Q, R, alg = r["A"], r["Q"], r["R"], r["alg"]
+        A0_, Q0_, R0_, alg = r["A"], r["Q"], r["R"], r["alg"]
         A_pin = torch.empty((n, m), dtype=torch.float64).pin_memory().t()
         A_pin.copy_(A_host)
-        Q_pin = torch.empty((Q.shape[1], Q.shape[0]), dtype=torch.float64).pin_memory().t()
-        R_pin = torch.empty((R.shape[1], R.shape[0]), dtype=torch.float64).pin_memory().t()
+        bufs = [(A0_, Q0_, R0_), (torch.empty_like(A0_), torch.empty_like(Q0_),
+                                  torch.empty_like(R0_))]
+        pins = [(torch.empty((Q0_.shape[1], Q0_.shape[0]), dtype=torch.float64).pin_memory().t(),
+                 torch.empty((R0_.shape[1], R0_.shape[0]), dtype=torch.float64).pin_memory().t())
+                for _ in range(2)]
+        s_h2d, s_d2h = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+        s_comp = torch.cuda.current_stream(dev)
+        ev = {k: [torch.cuda.Event() for _ in range(2)] for k in ("h2d", "comp", "d2h")}
+        used = [False, False]
 
-        def e2e_step():
-            A.copy_(A_pin, non_blocking=True)
+        def e2e_step(i):
+            b = i % 2
+            A, Q, R = bufs[b]
+            Qp, Rp = pins[b]
+            with torch.cuda.stream(s_h2d):
+                if used[b]:
+                    s_h2d.wait_event(ev["comp"][b])  # the kernels of step i-2 read A
+                A.copy_(A_pin, non_blocking=True)
+                ev["h2d"][b].record(s_h2d)
+            s_comp.wait_event(ev["h2d"][b])
+            if used[b]:
+                s_comp.wait_event(ev["d2h"][b])  # step i-2's factors are on the host
             mak.qr_compact_(A, (Q, R), alg)
-            Q_pin.copy_(Q, non_blocking=True)
-            R_pin.copy_(R, non_blocking=True)
+            ev["comp"][b].record(s_comp)
+            with torch.cuda.stream(s_d2h):
+                s_d2h.wait_event(ev["comp"][b])
+                Qp.copy_(Q, non_blocking=True)
+                Rp.copy_(R, non_blocking=True)
+                ev["d2h"][b].record(s_d2h)
+            used[b] = True
 
-        e2e_step()
+        e2e_step(0)
+        e2e_step(1)
+        torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
-        torch.cuda.synchronize()
-        k2 = max(1, min(args.steps, 3))
+        k2 = max(3, min(args.steps, 6))
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record()
-        for _ in range(k2):
-            e2e_step()
-        s1.record()
+        s0.record(s_comp)
+        s_h2d.wait_stream(s_comp)
+        s_d2h.wait_stream(s_comp)
+        for i in range(k2):
+            e2e_step(i)
+        s_comp.wait_stream(s_h2d)
+        s_comp.wait_stream(s_d2h)
+        s1.record(s_comp)
+        torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
-        torch.cuda.synchronize()
         ems = max_over_ranks(dist, s0.elapsed_time(s1) / k2, dev)
         out["e2e"] = {"value": round(job_tflops(ws, flops, ems), 5), "unit": "TFLOP/s",
                       "ms_per_step": round(ems, 3), "steps": k2,
-                      "h2d_bytes_per_step": int(A.numel() * 8),
-                      "d2h_bytes_per_step": int((Q.numel() + R.numel()) * 8)}
-        del A_pin, Q_pin, R_pin
+                      "h2d_bytes_per_step": int(A0_.numel() * 8),
+                      "d2h_bytes_per_step": int((Q0_.numel() + R0_.numel()) * 8),
+                      "overlap": "double-buffered: step i's copies overlap the kernels of "
+                                 "step i+1 (H2D and D2H streams, event-ordered)"}
+        del A_pin, pins, bufs
     del r
 
     # the plain FP64 kernels on the same input: the comparison the metric asks for
@@ -718,7 +757,8 @@ def batched_measure(mak, args, dev):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    for prec in ("native", "mixed"):
+    kinds = args.batched_kinds.split(",")
+    for prec in (("native", "mixed") if "qr" in kinds else ()):
         outs = mak.batched_qr_compact(work, copy_inputs=False, precision=prec)
 
         def restore():
@@ -743,15 +783,16 @@ def batched_measure(mak, args, dev):
             for w, (q, r) in zip(work, outs):
                 mak.qr_compact_(w, (q, r), precision=prec)
 
-        ms_loop = timed(loop, reps=1)
         res[f"qr_{prec}"] = {"graph_ms": round(ms_graph, 3), "blocks_per_s": round(nb * 1e3 / ms_graph, 1),
-                             "tflops": round(flops_qr / (ms_graph / 1e3) / 1e12, 4),
-                             "per_block_loop_ms": round(ms_loop, 3),
-                             "speedup_vs_loop": round(ms_loop / ms_graph, 2)}
+                             "tflops": round(flops_qr / (ms_graph / 1e3) / 1e12, 4)}
+        if not args.no_batched_loop:
+            ms_loop = timed(loop, reps=1)
+            res[f"qr_{prec}"].update({"per_block_loop_ms": round(ms_loop, 3),
+                                      "speedup_vs_loop": round(ms_loop / ms_graph, 2)})
         del g
     # polar (batched: up to 10 Newton iterations, each block stopped on the
     # device at the default tolerance) in both precisions
-    for prec in ("native", "mixed"):
+    for prec in (("native", "mixed") if "polar" in kinds else ()):
         def restore():
             for w, s_ in zip(work, srcs):
                 w.copy_(s_)
@@ -785,7 +826,7 @@ def batched_measure(mak, args, dev):
                                 if iters else None, "maxiter": 10,
                                 "max_back_err": back}
         del g
-    for kind in ("qr", "polar"):
+    for kind in kinds:
         a = res[f"{kind}_native"]["graph_ms"]
         b = res[f"{kind}_mixed"]["graph_ms"]
         res[f"{kind}_mixed_over_native"] = round(a / b, 3)
@@ -851,10 +892,18 @@ def sweep_measure(mak, args, dev):
     """Orthogonalisation sweep of a matrix-product canonicalisation: N
     ComplexF64 tensors of bond dimension 256 and physical dimension 4, each a
     1024 x 256 matrix (iid complex Gaussian).  One step = left_orth via QR of
-    every tensor (batched) + the QR pullback of the loss sum real(tr(D^H Q))
-    (dQ = D, dR = 0) for every tensor + left_polar of every tensor (batched,
-    at most 10 Newton iterations per block).  Wall-clock time per step on the host (the
-    pullbacks synchronize once each), both precisions."""
+    every tensor and left_polar of every tensor (batched calls, at most 10
+    Newton iterations stopped on the device), then the full pullback of the
+    scalar loss sum_i real(tr(D_i^H Q_i)) + real(tr(D_i^H W_i)) through both
+    (batched QR pullback: one host synchronization for all ranks; batched
+    polar pullback: none).  Three arithmetic modes on the same inputs:
+    "fp32" -- the Float32-class run: the tensors are converted to
+    ComplexF32 on the device (inside the timed step) and every kernel runs
+    in single precision, results compared with the FP64 ones at
+    sqrt(eps(Float32)) (the reference's precision(ComplexF32),
+    test/testsuite/TestSuite.jl:45); "mixed" -- ComplexF64 with the split
+    tensor-core products; "fp64" -- the plain FP64 kernels.  Wall-clock time
+    per step on the host (the ranks' read synchronizes)."""
     import numpy as np
     import torch
 
@@ -863,23 +912,58 @@ def sweep_measure(mak, args, dev):
     As = [_crandn(rng, 1024, 256, dev) for _ in range(N)]
     Ds = [_crandn(rng, 1024, 256, dev) for _ in range(N)]
     flops_qr = N * qr_flops(1024, 256, True)
-    res = {"workload": f"{N} ComplexF64 1024x256 tensors: batched QR + QR pullbacks + batched "
-                       f"polar (at most 10 Newton iterations, stopped on the device)", "qr_gflop": round(flops_qr / 1e9, 1)}
-    for prec in ("native", "mixed"):
-        def step():
-            outs = mak.batched_qr_compact(As, precision=prec)
-            for A, (Q, R), D in zip(As, outs, Ds):
-                dA = torch.zeros_like(A)
-                mak.qr_pullback_(dA, A, (Q, R), (D, None), precision=prec)
-            mak.batched_left_polar(As, precision=prec, maxiter=10)
+    res = {"workload": f"{N} ComplexF64 1024x256 tensors: batched QR + batched polar (<= 10 "
+                       f"Newton steps, stopped on the device) + batched pullbacks of "
+                       f"sum real(tr(D^H Q)) + real(tr(D^H W)) through both",
+           "qr_gflop": round(flops_qr / 1e9, 1)}
+    dAs_out = {}
+    for mode in ("fp64", "mixed", "fp32"):
+        prec = "mixed" if mode == "mixed" else "native"
+        dt = torch.complex64 if mode == "fp32" else torch.complex128
+
+        phases = {}
+
+        def mark(name, t):
+            torch.cuda.synchronize()
+            now = time.perf_counter()
+            phases[name] = round((now - t) * 1e3, 2)
+            return now
+
+        def step(timed_phases=False):
+            t = time.perf_counter()
+            X = [A.to(dt) for A in As] if dt != torch.complex128 else As
+            D = [d.to(dt) for d in Ds] if dt != torch.complex128 else Ds
+            QR = mak.batched_qr_compact(X, precision=prec)
+            if timed_phases:
+                t = mark("qr", t)
+            WP = mak.batched_left_polar(X, precision=prec, maxiter=10)
+            if timed_phases:
+                t = mark("polar", t)
+            dA = [torch.zeros_like(x) for x in X]
+            mak.batched_qr_pullback(dA, QR, [(d, None) for d in D], precision=prec)
+            if timed_phases:
+                t = mark("qr_pullback", t)
+            mak.batched_left_polar_pullback(dA, WP, [(d, None) for d in D], precision=prec)
+            if timed_phases:
+                mark("polar_pullback", t)
+            return dA
 
         step()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        step()
+        dA = step()
         torch.cuda.synchronize()
-        res[f"{prec}_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
-    res["mixed_over_native"] = round(res["native_ms"] / res["mixed_ms"], 3)
+        res[f"{mode}_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+        step(timed_phases=True)
+        res[f"{mode}_phases_ms"] = phases
+        dAs_out[mode] = dA
+    ref = dAs_out["fp64"]
+    for mode in ("mixed", "fp32"):
+        err = max(float(torch.linalg.norm(a.to(torch.complex128) - b) / torch.linalg.norm(b))
+                  for a, b in zip(dAs_out[mode], ref))
+        res[f"{mode}_dA_rel_vs_fp64"] = err
+        res[f"{mode}_over_fp64"] = round(res["fp64_ms"] / res[f"{mode}_ms"], 3)
+    res["fp32_tolerance"] = float(np.sqrt(np.finfo(np.float32).eps))
     return res
 
 
@@ -1025,6 +1109,19 @@ def run_batched_only(args):
     return 0
 
 
+def run_sweep_only(args):
+    """The orthogonalisation sweep alone (all three arithmetic modes)."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    mak = ge.load_package()
+    print(json.dumps(sweep_measure(mak, args, dev)), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1033,6 +1130,8 @@ def main():
         return run_gemm(args)
     if args.workload == "batched":
         return run_batched_only(args)
+    if args.workload == "sweep":
+        return run_sweep_only(args)
     if args.workload == "polar":
         return run_polar_only(args)
     return run_gb300(args)

@@ -324,6 +324,49 @@ int mak_batched_left_polar_workspace(const mak_batch_item* items, int nitems,
 int mak_batched_left_polar(const mak_batch_item* items, int nitems, const mak_polar_opts* opts,
                            void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream);
 
+/* Batched reverse rules over a list of blocks (the pullbacks of a whole
+ * block-sparse tensor, or of every tensor of an orthogonalisation sweep, in
+ * one call); no counterpart in the reference, whose callers loop
+ * qr_pullback! / left_polar_pullback! (src/pullbacks/qr.jl:73-120,
+ * src/pullbacks/polar.jl:7-29) over the blocks.  Items live in HOST memory
+ * and hold DEVICE pointers; element types may be mixed; blocks are scheduled
+ * over the same internal streams as the batched factorizations.  Each dA is
+ * ACCUMULATED into; dF1 / dF2 may be NULL (a zero tangent).  `infos` is a
+ * DEVICE array of nitems records.
+ *  - mak_batched_qr_pullback: qr_compact factors (F1 = Q m x min(m,n),
+ *    F2 = R min(m,n) x n, dF1 = dQ, dF2 = dR); the ranks of all blocks are
+ *    computed first and read with ONE host synchronization of `stream`.
+ *  - mak_batched_left_polar_pullback: F1 = W (m x n, m >= n), F2 = P (n x n),
+ *    dF1 = dW, dF2 = dP; the Sylvester sign iteration of every block runs a
+ *    fixed number of steps and stops on the device (no host
+ *    synchronization); infos[i].iterations / converged report it. */
+typedef struct {
+  int32_t dtype;     /* MAK_F64 / MAK_C64 / MAK_F32 / MAK_C32                  */
+  int32_t reserved;
+  int64_t m, n;
+  void* dA;          /* m x n, accumulated into                               */
+  int64_t ldda;
+  const void* F1;    /* Q or W                                                */
+  int64_t ld1;
+  const void* F2;    /* R or P                                                */
+  int64_t ld2;
+  const void* dF1;   /* dQ or dW, or NULL                                     */
+  int64_t ldd1;
+  const void* dF2;   /* dR or dP, or NULL                                     */
+  int64_t ldd2;
+} mak_batch_pullback_item;
+
+int mak_batched_qr_pullback_workspace(const mak_batch_pullback_item* items, int nitems,
+                                      const mak_pullback_opts* opts, size_t* bytes);
+int mak_batched_qr_pullback(const mak_batch_pullback_item* items, int nitems,
+                            const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                            mak_info* infos, mak_stream_t stream);
+int mak_batched_left_polar_pullback_workspace(const mak_batch_pullback_item* items, int nitems,
+                                              const mak_pullback_opts* opts, size_t* bytes);
+int mak_batched_left_polar_pullback(const mak_batch_pullback_item* items, int nitems,
+                                    const mak_pullback_opts* opts, void* work, size_t work_bytes,
+                                    mak_info* infos, mak_stream_t stream);
+
 /* ------------------------------------------------------------ pullbacks ---
  * qr_pullback!(dA, A, (Q, R), (dQ, dR); rank_atol, gauge_atol)
  * Replaces the reference's qr_pullback! (src/pullbacks/qr.jl:73-120) with

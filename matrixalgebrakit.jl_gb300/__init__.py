@@ -49,9 +49,11 @@ __all__ += ["qr_pullback_", "left_polar_pullback_", "right_polar_pullback_", "qr
             "lq_pullback_", "lq_null_pullback_",
             "left_polar_pushforward_", "right_polar_pushforward_"]
 
-from .batched import batched_left_polar, batched_qr_compact  # noqa: E402
+from .batched import (batched_left_polar, batched_left_polar_pullback,  # noqa: E402
+                      batched_qr_compact, batched_qr_pullback)
 
-__all__ += ["batched_qr_compact", "batched_left_polar"]
+__all__ += ["batched_qr_compact", "batched_left_polar", "batched_qr_pullback",
+            "batched_left_polar_pullback"]
 
 from .algorithms import RightOrthViaLQ, RightOrthViaPolar  # noqa: E402
 from .orthnull import (batched_left_orth, batched_project_isometric, left_null,  # noqa: E402

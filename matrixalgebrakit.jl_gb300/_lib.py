@@ -173,3 +173,20 @@ SIGNATURES["mak_batched_left_polar_workspace"] = (C.c_int, [C.POINTER(mak_batch_
                                                             C.POINTER(_sz)])
 SIGNATURES["mak_batched_left_polar"] = (C.c_int, [C.POINTER(mak_batch_item), C.c_int,
                                                   C.POINTER(mak_polar_opts), _p, _sz, _p, _p])
+
+
+class mak_batch_pullback_item(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("reserved", C.c_int32), ("m", C.c_int64),
+                ("n", C.c_int64), ("dA", C.c_void_p), ("ldda", C.c_int64), ("F1", C.c_void_p),
+                ("ld1", C.c_int64), ("F2", C.c_void_p), ("ld2", C.c_int64),
+                ("dF1", C.c_void_p), ("ldd1", C.c_int64), ("dF2", C.c_void_p),
+                ("ldd2", C.c_int64)]
+
+
+for _nm in ("qr", "left_polar"):
+    SIGNATURES[f"mak_batched_{_nm}_pullback_workspace"] = (
+        C.c_int, [C.POINTER(mak_batch_pullback_item), C.c_int, C.POINTER(mak_pullback_opts),
+                  C.POINTER(_sz)])
+    SIGNATURES[f"mak_batched_{_nm}_pullback"] = (
+        C.c_int, [C.POINTER(mak_batch_pullback_item), C.c_int, C.POINTER(mak_pullback_opts),
+                  _p, _sz, _p, _p])

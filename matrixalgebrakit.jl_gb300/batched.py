@@ -11,6 +11,7 @@ result is identical to the per-block calls.
 from __future__ import annotations
 
 import ctypes as ct
+import warnings
 
 import torch
 
@@ -102,3 +103,91 @@ def batched_left_polar(As, alg=None, copy_inputs=True, outs=None, _capturing=Fal
     if _info is not None and res is not None:
         _info.extend(int(r.iterations) for r in res)
     return outs
+
+
+def _pb_items(dAs, F1s, F2s, dF1s, dF2s):
+    arr = (_lib.mak_batch_pullback_item * len(dAs))()
+    for i, (dA, F1, F2, d1, d2) in enumerate(zip(dAs, F1s, F2s, dF1s, dF2s)):
+        m, n = dA.shape
+        arr[i] = _lib.mak_batch_pullback_item(
+            DTYPE_CODE[dA.dtype], 0, m, n, dA.data_ptr(), ld_or_raise(dA, "dA"),
+            F1.data_ptr(), ld_or_raise(F1, "F1"), F2.data_ptr(), ld_or_raise(F2, "F2"),
+            d1.data_ptr() if d1 is not None else None,
+            ld_or_raise(d1, "dF1") if d1 is not None else 1,
+            d2.data_ptr() if d2 is not None else None,
+            ld_or_raise(d2, "dF2") if d2 is not None else 1)
+    return arr
+
+
+def _run_pb(kind, dAs, F1s, F2s, dF1s, dF2s, precision, rank_atol=None, gauge_atol=None,
+            capturing=False):
+    from .pullbacks import _opts
+
+    if not dAs:
+        return []
+    dev = dAs[0].device
+    for lst, nm in ((dAs, "dA"), (F1s, "F1"), (F2s, "F2")):
+        for X in lst:
+            check_cuda_tensor(X, nm)
+            if X.device != dev:
+                raise ArgumentError("all blocks must live on one device")
+    for dA, F1 in zip(dAs, F1s):
+        if dA.dtype != F1.dtype:
+            raise ArgumentError("element types of dA and the factors differ")
+    items = _pb_items(dAs, F1s, F2s, dF1s, dF2s)
+    opts = _opts(rank_atol, gauge_atol, precision)
+    L = lib()
+    wsfn = getattr(L, f"mak_batched_{kind}_pullback_workspace")
+    runfn = getattr(L, f"mak_batched_{kind}_pullback")
+    nbytes = ct.c_size_t(0)
+    check_rc(wsfn(items, len(dAs), ct.byref(opts), ct.byref(nbytes)), wsfn.__name__)
+    with torch.cuda.device(dev):
+        work = workspace(nbytes.value, dev)
+        infos = torch.zeros(len(dAs) * INFO_BYTES, dtype=torch.uint8, device=dev)
+        rc = runfn(items, len(dAs), ct.byref(opts), work.data_ptr(), nbytes.value,
+                   infos.data_ptr(), stream_handle(dev))
+        check_rc(rc, runfn.__name__)
+        if capturing:
+            return None
+        res = _read_infos(infos, len(dAs))
+    for i, inf in enumerate(res):
+        if inf.status != 0:
+            raise RuntimeError(f"{runfn.__name__}: block {i}: device status {inf.status}")
+    return res
+
+
+def batched_qr_pullback(dAs, QRs, dQRs, precision="native", rank_atol=None, gauge_atol=None,
+                        _info=None):
+    """``qr_pullback!`` of every block (qr_compact factors): ``dA_i +=`` the
+    pullback of ``(dQ_i, dR_i)`` at ``(Q_i, R_i)``; one host synchronization
+    for the whole batch (the blocks' ranks).  ``_info`` (a list) receives
+    each block's rank."""
+    res = _run_pb("qr", dAs, [q for q, _ in QRs], [r for _, r in QRs],
+                  [d for d, _ in dQRs], [d for _, d in dQRs], precision, rank_atol, gauge_atol)
+    if _info is not None:
+        _info.extend(int(r.rank) for r in res)
+    for i, r in enumerate(res):
+        if r.gauge > r.gauge_atol:
+            warnings.warn(f"block {i}: `qr` cotangents sensitive to gauge choice: "
+                          f"(|Δgauge| = {r.gauge})", RuntimeWarning, stacklevel=2)
+    return dAs
+
+
+def batched_left_polar_pullback(dAs, WPs, dWPs, precision="native", _capturing=False,
+                                _info=None):
+    """``left_polar_pullback!`` of every block: ``dA_i +=`` the pullback of
+    ``(dW_i, dP_i)`` at ``(W_i, P_i)``; no host synchronization (the
+    Sylvester sign iterations stop on the device), so the call can be
+    captured in a CUDA graph.  ``_info`` (a list) receives each block's sign
+    iteration count."""
+    res = _run_pb("left_polar", dAs, [w for w, _ in WPs], [p for _, p in WPs],
+                  [d for d, _ in dWPs], [d for _, d in dWPs], precision, capturing=_capturing)
+    if res is None:
+        return dAs
+    if _info is not None:
+        _info.extend(int(r.iterations) for r in res)
+    for i, r in enumerate(res):
+        if not r.converged and dAs[i].shape[1] > 0:
+            raise RuntimeError(f"mak_batched_left_polar_pullback: block {i}: the Sylvester "
+                               f"sign iteration did not converge in {r.iterations} steps")
+    return dAs

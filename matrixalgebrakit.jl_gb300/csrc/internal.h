@@ -2,6 +2,7 @@
 // libmak_gb300.so.  Each template is explicitly instantiated for double,
 // zcomplex, float and ccomplex in the .cu file that defines it.
 #pragma once
+#include <cstdlib>
 #include "mak_common.cuh"
 
 namespace mak {
@@ -23,6 +24,36 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
                 Arena& ar, mak_info* info);
 
 int info_reset(cudaStream_t st, mak_info* info);
+
+// qr_pullback! (dA += ...); known_p >= 0 skips the host read of the rank
+template <class T>
+int qr_pullback_run(cudaStream_t st, int64_t m, int64_t n, int full, T* dA, int64_t ldda,
+                    const T* Q, int64_t ldq, const T* R, int64_t ldr, const T* dQ, int64_t lddq,
+                    const T* dR, int64_t lddr, double rank_atol, double gauge_atol, int precision,
+                    Arena& ar, mak_info* info, int known_p = -1);
+// numerical rank of the k x n triangular R into the device int *p_out
+template <class T>
+int qr_rank_run(cudaStream_t st, int64_t k, int64_t n, const T* R, int64_t ldr, double rank_atol,
+                Arena& ar, int* p_out);
+// left_polar_pullback! (dA += ...); maxiter < 0: the Sylvester sign
+// iteration runs -maxiter steps stopped on the device (no host sync)
+template <class T>
+int polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldda, const T* W,
+                       int64_t ldw, const T* P, int64_t ldp, const T* dW, int64_t lddw,
+                       const T* dP, int64_t lddp, int maxiter, int precision, Arena& ar,
+                       mak_info* info);
+
+// A numeric tuning parameter: the environment variable `name` when it is set
+// and within [lo, hi], else `dflt`.  Call sites keep the value in a
+// function-local static, so it is read once per process.
+inline double env_param(const char* name, double dflt, double lo, double hi) {
+  const char* e = getenv(name);
+  if (e && *e) {
+    const double x = atof(e);
+    if (x >= lo && x <= hi) return x;
+  }
+  return dflt;
+}
 
 // Look-ahead (QR and Gauss-Jordan): a high-priority side stream factors the
 // next block while the main stream updates the far columns.  On/off for

@@ -283,15 +283,17 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
   // mixed precision: 128-wide block columns, eliminated with 32-wide panels
   // whose updates stay inside the block; the other columns then receive one
   // rank-128 update through the split-precision tensor-core GEMM
-  // the 128-wide blocking only for large inverses (n^2 128 >= 2^29 multiply-
-  // adds, complex counted 4x: n >= 2048 real, n >= 1024 complex); below that
-  // its extra launches and split passes cost more than the tensor cores
-  // save (measured on batches of blocks with n <= 1024), and the native
-  // elimination runs even when mixed precision is asked for (a gate of its
-  // own: the general split-product gate does not move it)
+  // the 128-wide blocking from n^2 128 >= 2^25 multiply-adds (complex
+  // counted 4x: n >= 512 real, n >= 256 complex; MAK_GJ_SPLIT_MIN overrides
+  // it).  Below that the native elimination runs even when mixed precision
+  // is asked for (a gate of its own: the general split-product gate does not
+  // move it).  Measured on the 300 uneven blocks (mixed polar, CUDA-graph
+  // replay, 16 streams): gate 2^29 / 2^25 / 2^23 gave 2.23 / 1.80 / 1.75 s;
+  // the launches the lower gates add only cost when they are not replayed
+  // from a graph (the same batch issued eagerly: 2.68 / 5.47 / 5.64 s).
+  static const double gate = env_param("MAK_GJ_SPLIT_MIN", 33554432.0 /* 2^25 */, 1.0, 1e18);
   const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8 &&
-                     (traits<T>::cpx ? 4.0 : 1.0) * (double)n * (double)n * GJ_OUTER_NB >=
-                         536870912.0;  // 2^29
+                     (traits<T>::cpx ? 4.0 : 1.0) * (double)n * (double)n * GJ_OUTER_NB >= gate;
   const int NBO = mixed ? GJ_OUTER_NB : GJ_NB;
   int* piv = ar.take<int>(n > 0 ? n : 1);
   // per-CTA pivot partials and candidate rows, double-buffered by column parity
@@ -600,14 +602,17 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
   const bool ns_ok = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8;
   T* Yn = ns_ok ? ar.take<T>((size_t)n * n + 1) : nullptr;  // Newton-Schulz product
   // Without host synchronization (the batched driver) both step kinds are
-  // launched every iteration and flags let one run.  There the finish pays
-  // only for 256 <= n <= 384 (measured): below, the extra launches cost more
-  // than the Gauss-Jordan inverses saved; above, its two split products under
-  // the batch's per-stream CTA budget cost about an inverse each and hold
-  // their SMs against the other streams' panels, while the finish takes one
-  // step more than Newton from the switch point.  The host-checked loop
-  // launches just the step it takes and uses the finish at every n.
-  const bool ns_fixed_ok = ns_ok && n >= 256 && n <= 384;
+  // launched every iteration and flags let one run.  There the finish is
+  // used from n >= 256 (MAK_NS_FIXED_MIN_N / _MAX_N override the range):
+  // below, the extra launches cost more than the Gauss-Jordan inverses
+  // saved.  Measured on the 300 uneven blocks (mixed, CUDA-graph replay, 16
+  // streams, tensor-core Gauss-Jordan updates from 2^25): finish for
+  // 256 <= n <= 384 only 1.80 s, for every n >= 256 1.54 s.  The
+  // host-checked loop launches just the step it takes and uses the finish
+  // at every n.
+  static const int ns_lo = (int)env_param("MAK_NS_FIXED_MIN_N", 256, 0, 1 << 30);
+  static const int ns_hi = (int)env_param("MAK_NS_FIXED_MAX_N", 1 << 30, 0, 1 << 30);
+  const bool ns_fixed_ok = ns_ok && n >= ns_lo && n <= ns_hi;
   T* Qw = (m > n) ? ar.take<T>((size_t)m * n) : nullptr;
   T* Rw = (m > n) ? ar.take<T>((size_t)n * n) : nullptr;
   T* A0 = (m == n && want_p) ? ar.take<T>((size_t)n * n) : nullptr;

@@ -133,8 +133,9 @@ __global__ void gather_cols_kernel(int n, const T* X, int64_t ldx, const int* ip
 //   A <- (mu A + Ai/mu)/2,  C <- (mu C + Tm/mu)/2,  *dnorm += |A_new - A_old|^2 (partial)
 template <class T>
 __global__ void sign_update_kernel(int64_t nn, T* A, const T* Ai, T* Cm, const T* Tm,
-                                   const real_t<T>* nrm2, real_t<T>* dpart) {
+                                   const real_t<T>* nrm2, real_t<T>* dpart, const int* skip) {
   using Rr = real_t<T>;
+  if (skipped(skip)) return;
   __shared__ Rr sh[32];
   const Rr mu = sqrt(sqrt(nrm2[1] / nrm2[0]));
   const Rr imu = Rr(1) / mu;
@@ -149,6 +150,20 @@ __global__ void sign_update_kernel(int64_t nn, T* A, const T* Ai, T* Cm, const T
   }
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) dpart[blockIdx.x] = acc;
+}
+
+// Device stop of the sign iteration without host synchronization: w[0] is
+// the stop flag the later iterations' kernels read on entry, w[1] counts the
+// iterations taken (NaN stops, as the host-checked loop does).
+template <class R>
+__global__ void sign_stop_kernel(const R* dnorm2, R tol, int* w) {
+  if (w[0]) return;
+  w[1] += 1;
+  if (!(sqrt(*dnorm2) > tol)) w[0] = 1;
+}
+__global__ void info_sign_fixed_kernel(mak_info* info, const int* w) {
+  info->iterations = w[1];
+  info->converged = w[0];
 }
 
 template <class R>
@@ -186,11 +201,13 @@ __global__ void info_pullback_kernel(mak_info* info, int p, int iters, const rea
 }
 
 // -------------------------------------------------------------- QR pullback --
+// known_p >= 0: the numerical rank was computed beforehand (qr_rank_run,
+// e.g. for a whole batch at once) and no host synchronization is needed.
 template <class T>
 int qr_pullback_run(cudaStream_t st, int64_t m, int64_t n, int full, T* dA, int64_t ldda,
                     const T* Q, int64_t ldq, const T* R, int64_t ldr, const T* dQ, int64_t lddq,
                     const T* dR, int64_t lddr, double rank_atol, double gauge_atol, int precision,
-                    Arena& ar, mak_info* info) {
+                    Arena& ar, mak_info* info, int known_p) {
   using Rr = real_t<T>;
   const int64_t k = m < n ? m : n;
   const int64_t qc = full ? m : k;
@@ -239,9 +256,11 @@ int qr_pullback_run(cudaStream_t st, int64_t m, int64_t n, int full, T* dA, int6
   note_launch();
   qr_rank_kernel<T><<<1, 256, 0, st>>>((int)k, R, ldr, maxR, rank_atol, pdev, ratol);
   MAK_CUDA_TRY(cudaGetLastError());
-  int p = 0;
-  MAK_CUDA_TRY(cudaMemcpyAsync(&p, pdev, sizeof(int), cudaMemcpyDeviceToHost, st));
-  MAK_CUDA_TRY(cudaStreamSynchronize(st));
+  int p = known_p;
+  if (p < 0) {
+    MAK_CUDA_TRY(cudaMemcpyAsync(&p, pdev, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MAK_CUDA_TRY(cudaStreamSynchronize(st));
+  }
 
   // gauge tolerance: eps(max|dQ|)^(3/4) (0 for a zero tangent)
   if (gauge_atol >= 0) {
@@ -322,6 +341,36 @@ int qr_pullback_run(cudaStream_t st, int64_t m, int64_t n, int full, T* dA, int6
   return 0;
 }
 
+// The numerical rank alone (reference qr_rank, src/pullbacks/qr.jl:1-2,
+// tolerance eps(norm(R, Inf))^(3/4) when rank_atol < 0) into the device int
+// *p_out: what qr_pullback_run computes first, for callers that read the
+// ranks of many factorizations with one host synchronization.
+template <class T>
+int qr_rank_run(cudaStream_t st, int64_t k, int64_t n, const T* R, int64_t ldr, double rank_atol,
+                Arena& ar, int* p_out) {
+  using Rr = real_t<T>;
+  Rr* scal = ar.take<Rr>(RED_CTAS + 4);
+  if (ar.base == nullptr) return 0;
+  if (!ar.ok()) return MAK_ERR_WORKSPACE;
+  MAK_CUDA_TRY(cudaMemsetAsync(scal + RED_CTAS, 0, 4 * sizeof(Rr), st));
+  MAK_TRY(reduce_mat<T>(st, k, n, R, ldr, 1, scal, scal + RED_CTAS));
+  note_launch();
+  qr_rank_kernel<T><<<1, 256, 0, st>>>((int)k, R, ldr, scal + RED_CTAS, rank_atol, p_out,
+                                       scal + RED_CTAS + 1);
+  return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
+}
+
+#define MAK_INST_PB(T)                                                                         \
+  template int qr_pullback_run<T>(cudaStream_t, int64_t, int64_t, int, T*, int64_t, const T*,  \
+                                  int64_t, const T*, int64_t, const T*, int64_t, const T*,     \
+                                  int64_t, double, double, int, Arena&, mak_info*, int);       \
+  template int qr_rank_run<T>(cudaStream_t, int64_t, int64_t, const T*, int64_t, double,       \
+                              Arena&, int*);
+MAK_INST_PB(double)
+MAK_INST_PB(zcomplex)
+MAK_INST_PB(float)
+MAK_INST_PB(ccomplex)
+
 // ----------------------------------------------------------- polar pullback --
 // Scratch of the device Sylvester solve (and of the products around it).
 template <class T>
@@ -329,6 +378,7 @@ struct SylScratch {
   real_t<T>* scal;
   T *Mm, *Ak, *Ck, *Ai, *Tm, *Y, *Pinv;
   int* iperm;
+  int* stopw;  // device stop of the sign iteration: [0] stop flag, [1] iterations
   char* tail;
   size_t tail_bytes;
 };
@@ -346,6 +396,7 @@ static SylScratch<T> syl_take(Arena& ar, cudaStream_t st, int64_t m, int64_t n, 
   s.Tm = ar.take<T>(nn + 1);
   s.Y = ar.take<T>((size_t)m * n + 1);
   s.iperm = ar.take<int>(n + 1);
+  s.stopw = ar.take<int>(2);
   size_t gj_ws = 0, oz_ws = 0;
   {
     Arena meas(nullptr, 0);
@@ -369,13 +420,19 @@ static SylScratch<T> syl_take(Arena& ar, cudaStream_t st, int64_t m, int64_t n, 
 // carried on its two blocks (A_k, C_k): A_{k+1} = (A_k + A_k^-1)/2,
 // C_{k+1} = (C_k + A_k^-1 C_k A_k^-1)/2 from A_0 = P, C_0 = -(M - M^H);
 // the solution is X = -C_inf / 2.  M is read from s.Mm (ld n); P^-1 (the
-// first iterate's inverse) is left in s.Pinv; X goes to s.Tm.  The host
-// synchronizes once per iteration for the stopping test.
+// first iterate's inverse) is left in s.Pinv; X goes to s.Tm.  maxiter > 0:
+// the host synchronizes once per iteration for the stopping test.
+// maxiter < 0: no host synchronization (CUDA-graph capturable): -maxiter
+// iterations are launched and the loop stops on the device once the test
+// is met (the stopped iterations' kernels return at once); *iters is then
+// -1 and the count and the outcome stay in s.stopw.
 template <class T>
 static int syl_solve(cudaStream_t st, int64_t n, const T* P, int64_t ldp, int maxiter,
                      int precision, SylScratch<T>& s, mak_info* info, int* iters) {
   using Rr = real_t<T>;
   const size_t nn = (size_t)n * n;
+  const bool fixed = maxiter < 0;
+  if (fixed) maxiter = -maxiter;
   int* status = &info->status;
   Rr* red = s.scal;
   Rr* nrm2 = s.scal + RED_CTAS;  // [0] ||A||^2, [1] ||Ai||^2, [2] ||dA||^2
@@ -406,7 +463,9 @@ static int syl_solve(cudaStream_t st, int64_t n, const T* P, int64_t ldp, int ma
   MAK_TRY(copy_mat<T>(st, n, n, P, ldp, s.Ak, n));
   const Rr tol = (sizeof(Rr) == 8 ? Rr(1e-13) : Rr(1e-6)) * sqrt((Rr)n);
   int it = 0;
+  if (fixed) MAK_CUDA_TRY(cudaMemsetAsync(s.stopw, 0, 2 * sizeof(int), st));
   for (it = 1; it <= maxiter; it++) {
+    SkipScope skip(fixed ? s.stopw : skip_flag());
     MAK_TRY(inverse(s.Ak, s.Ai));
     if (it == 1) MAK_TRY(copy_mat<T>(st, n, n, s.Ai, n, s.Pinv, n));
     MAK_TRY(reduce_mat<T>(st, n, n, s.Ak, n, 0, red, nrm2));
@@ -416,19 +475,26 @@ static int syl_solve(cudaStream_t st, int64_t n, const T* P, int64_t ldp, int ma
     MAK_TRY(G(n, n, n, one_<T>(), opnd<T>(s.Y, n), opnd<T>(s.Ai, n), zero_<T>(), s.Tm, n));
     const unsigned gr = g1 < RED_CTAS ? g1 : RED_CTAS;
     note_launch();
-    sign_update_kernel<T><<<gr, 256, 0, st>>>((int64_t)nn, s.Ak, s.Ai, s.Ck, s.Tm, nrm2, red);
+    sign_update_kernel<T><<<gr, 256, 0, st>>>((int64_t)nn, s.Ak, s.Ai, s.Ck, s.Tm, nrm2, red,
+                                               skip_flag());
     MAK_CUDA_TRY(cudaGetLastError());
     note_launch();
     reduce_final_kernel<Rr><<<1, 256, 0, st>>>((int)gr, red, 0, nrm2 + 2);
     MAK_CUDA_TRY(cudaGetLastError());
-    MAK_TRY(herm_project<T>(st, n, s.Ak, n));
+    MAK_TRY(herm_project<T>(st, n, s.Ak, n));  // idempotent once A is Hermitian
+    if (fixed) {
+      note_launch();
+      sign_stop_kernel<Rr><<<1, 1, 0, st>>>(nrm2 + 2, tol, s.stopw);
+      MAK_CUDA_TRY(cudaGetLastError());
+      continue;
+    }
     Rr dnorm2 = 0;
     MAK_CUDA_TRY(cudaMemcpyAsync(&dnorm2, nrm2 + 2, sizeof(Rr), cudaMemcpyDeviceToHost, st));
     MAK_CUDA_TRY(cudaStreamSynchronize(st));
     if (!(sqrt(dnorm2) > tol)) break;
   }
   if (it > maxiter) it = maxiter;
-  *iters = it;
+  *iters = fixed ? -1 : it;
   // X = -C_inf / 2
   note_launch();
   scale_copy_kernel<T><<<g1, 256, 0, st>>>((int64_t)nn, s.Ck, Rr(-0.5), s.Tm);
@@ -490,6 +556,11 @@ int polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldd
   note_launch();
   info_pullback_kernel<T><<<1, 1, 0, st>>>(info, (int)n, it, nullptr, nullptr);
   MAK_CUDA_TRY(cudaGetLastError());
+  if (it < 0) {
+    note_launch();
+    info_sign_fixed_kernel<<<1, 1, 0, st>>>(info, s.stopw);
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
   return 0;
 }
 
@@ -530,6 +601,15 @@ int polar_pushforward_run(cudaStream_t st, int64_t m, int64_t n, const T* dA, in
   MAK_CUDA_TRY(cudaGetLastError());
   return 0;
 }
+
+#define MAK_INST_PPB(T)                                                                        \
+  template int polar_pullback_run<T>(cudaStream_t, int64_t, int64_t, T*, int64_t, const T*,    \
+                                     int64_t, const T*, int64_t, const T*, int64_t, const T*,  \
+                                     int64_t, int, int, Arena&, mak_info*);
+MAK_INST_PPB(double)
+MAK_INST_PPB(zcomplex)
+MAK_INST_PPB(float)
+MAK_INST_PPB(ccomplex)
 
 constexpr int SIGN_MAXITER = 60;
 
