@@ -902,8 +902,11 @@ def sweep_measure(mak, args, dev):
     in single precision, results compared with the FP64 ones at
     sqrt(eps(Float32)) (the reference's precision(ComplexF32),
     test/testsuite/TestSuite.jl:45); "mixed" -- ComplexF64 with the split
-    tensor-core products; "fp64" -- the plain FP64 kernels.  Wall-clock time
-    per step on the host (the ranks' read synchronizes)."""
+    tensor-core products; "fp64" -- the plain FP64 kernels.  The forward and
+    the polar pullback are captured once as CUDA graphs and replayed every
+    step (they synchronize nothing); the QR pullback runs between them (it
+    reads all blocks' ranks with one host synchronization).  Wall-clock time
+    per step on the host."""
     import numpy as np
     import torch
 
@@ -920,43 +923,76 @@ def sweep_measure(mak, args, dev):
     for mode in ("fp64", "mixed", "fp32"):
         prec = "mixed" if mode == "mixed" else "native"
         dt = torch.complex64 if mode == "fp32" else torch.complex128
+        # device buffers of the step; the forward (batched QR + batched polar)
+        # and the polar pullback synchronize nothing and are replayed from
+        # CUDA graphs, the QR pullback (one host read of all ranks) runs
+        # between them
+        X = [torch.empty_like(A, dtype=dt) for A in As]
+        D = [torch.empty_like(d, dtype=dt) for d in Ds]
+        Xw = [torch.empty_like(x) for x in X]
+        Xp = [torch.empty_like(x) for x in X]
+        dA = [torch.empty_like(x) for x in X]
 
+        def load():
+            for x, a, xw, xp in zip(X, As, Xw, Xp):
+                x.copy_(a)  # the Float32-class run converts here
+                xw.copy_(x)
+                xp.copy_(x)
+            for d, s_ in zip(D, Ds):
+                d.copy_(s_)
+            for g in dA:
+                g.zero_()
+
+        load()
+        QR = mak.batched_qr_compact(Xw, copy_inputs=False, precision=prec)
+        WP = mak.batched_left_polar(Xp, copy_inputs=False, precision=prec, maxiter=10)
+        mak.batched_left_polar_pullback(dA, WP, [(d, None) for d in D], precision=prec)
+        torch.cuda.synchronize()
+        g_fwd, g_pb = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+        cs = torch.cuda.Stream()
+        cs.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(cs):
+            with torch.cuda.graph(g_fwd, stream=cs):
+                load()
+                mak.batched_qr_compact(Xw, copy_inputs=False, outs=QR, precision=prec,
+                                       _capturing=True)
+                mak.batched_left_polar(Xp, copy_inputs=False, outs=WP, precision=prec,
+                                       maxiter=10, _capturing=True)
+            with torch.cuda.graph(g_pb, stream=cs):
+                mak.batched_left_polar_pullback(dA, WP, [(d, None) for d in D],
+                                                precision=prec, _capturing=True)
+        torch.cuda.current_stream().wait_stream(cs)
         phases = {}
-
-        def mark(name, t):
-            torch.cuda.synchronize()
-            now = time.perf_counter()
-            phases[name] = round((now - t) * 1e3, 2)
-            return now
 
         def step(timed_phases=False):
             t = time.perf_counter()
-            X = [A.to(dt) for A in As] if dt != torch.complex128 else As
-            D = [d.to(dt) for d in Ds] if dt != torch.complex128 else Ds
-            QR = mak.batched_qr_compact(X, precision=prec)
+            g_fwd.replay()
             if timed_phases:
-                t = mark("qr", t)
-            WP = mak.batched_left_polar(X, precision=prec, maxiter=10)
-            if timed_phases:
-                t = mark("polar", t)
-            dA = [torch.zeros_like(x) for x in X]
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                phases["forward"] = round((t1 - t) * 1e3, 2)
+                t = t1
             mak.batched_qr_pullback(dA, QR, [(d, None) for d in D], precision=prec)
             if timed_phases:
-                t = mark("qr_pullback", t)
-            mak.batched_left_polar_pullback(dA, WP, [(d, None) for d in D], precision=prec)
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                phases["qr_pullback"] = round((t1 - t) * 1e3, 2)
+                t = t1
+            g_pb.replay()
             if timed_phases:
-                mark("polar_pullback", t)
-            return dA
+                torch.cuda.synchronize()
+                phases["polar_pullback"] = round((time.perf_counter() - t) * 1e3, 2)
 
         step()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        dA = step()
+        step()
         torch.cuda.synchronize()
         res[f"{mode}_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+        dAs_out[mode] = [g.clone() for g in dA]
         step(timed_phases=True)
         res[f"{mode}_phases_ms"] = phases
-        dAs_out[mode] = dA
+        del g_fwd, g_pb
     ref = dAs_out["fp64"]
     for mode in ("mixed", "fp32"):
         err = max(float(torch.linalg.norm(a.to(torch.complex128) - b) / torch.linalg.norm(b))

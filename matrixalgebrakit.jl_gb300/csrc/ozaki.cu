@@ -53,11 +53,22 @@
 
 namespace mak {
 
-constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = 16;
+// K per pipeline stage (16: 32-byte swizzled rows, 32: 64-byte rows) and
+// the number of stages; MAK_OZ_BK / MAK_OZ_STAGES select another tiling at
+// build time (the shared memory of all stages must stay within 227 KB)
+#ifndef MAK_OZ_BK
+#define MAK_OZ_BK 16
+#endif
+#ifndef MAK_OZ_STAGES
+#define MAK_OZ_STAGES 4
+#endif
+constexpr int OZ_BM = 128, OZ_BN = 64, OZ_BK = MAK_OZ_BK;
+static_assert(OZ_BK == 16 || OZ_BK == 32, "K step of 16 or 32");
 constexpr int OZ_KSTEPS_PER_CHUNK = 512 / OZ_BK;  // 512 of K between exact flushes
+constexpr int OZ_SMALL_CHUNK = 128 / OZ_BK;       // K <= 128: one short exact chunk
 constexpr int OZ_ROW_BYTES = OZ_BK * 2;           // one swizzled K row of a plane tile
 constexpr int OZ_BITS = 7;              // bits per (balanced) digit plane
-constexpr int OZ_STAGES = 4;           // 4 x 48 KB: finer stages keep more loads in flight
+constexpr int OZ_STAGES = MAK_OZ_STAGES;  // 4 x 48 KB (K step 16): finer stages keep more loads in flight
 constexpr int OZ_EPI_WARPS = 8;         // two warps per TMEM lane quadrant
 constexpr int OZ_THREADS = 32 * (OZ_EPI_WARPS + 2);  // + TMA warp + MMA warp
 constexpr int OZ_TMA_WARP = OZ_EPI_WARPS, OZ_MMA_WARP = OZ_EPI_WARPS + 1;
@@ -814,9 +825,9 @@ template <int S>
 static void oz_set_attr() {
   static PerDevice<int> pd;
   pd.get([] {
-    cudaFuncSetAttribute(oz_gemm_kernel<S, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(oz_gemm_kernel<S, OZ_KSTEPS_PER_CHUNK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)oz_smem_bytes<S>());
-    cudaFuncSetAttribute(oz_gemm_kernel<S, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(oz_gemm_kernel<S, OZ_SMALL_CHUNK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)oz_smem_bytes<S>());
     return 1;
   });
@@ -927,9 +938,9 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
     const int grid = (int)(nwork < cap ? nwork : cap);
     note_launch();
     if (nkt_total * OZ_BK <= 128)  // one short chunk: the FFMA conversion
-      oz_gemm_kernel<S, 8><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
+      oz_gemm_kernel<S, OZ_SMALL_CHUNK><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
     else
-      oz_gemm_kernel<S, 32><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
+      oz_gemm_kernel<S, OZ_KSTEPS_PER_CHUNK><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
     MAK_CUDA_TRY(cudaGetLastError());
   }
   if (part) {
