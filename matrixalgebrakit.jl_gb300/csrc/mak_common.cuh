@@ -305,6 +305,38 @@ __device__ __forceinline__ bool panel_sync(unsigned* bar, unsigned nblocks, int*
 // largest cluster the panels use (the portable limit)
 constexpr int kPanelClusterMax = 8;
 
+// Loads from the shared memory of CTA `rank` of the calling thread's
+// cluster (distributed shared memory): `p` is the address of the same
+// variable in the caller's own shared memory.  Used by the cluster variant
+// of the panels to read the other CTAs' partials after the cluster barrier
+// instead of a round trip through L2.
+__device__ __forceinline__ uint32_t dsmem_addr(const void* p, unsigned rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+               : "=r"(r)
+               : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ double dsmem_ld(const double* p, unsigned rank) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(dsmem_addr(p, rank)) : "memory");
+  return v;
+}
+__device__ __forceinline__ float dsmem_ld(const float* p, unsigned rank) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(dsmem_addr(p, rank)) : "memory");
+  return v;
+}
+__device__ __forceinline__ int dsmem_ld(const int* p, unsigned rank) {
+  int v;
+  asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(dsmem_addr(p, rank)) : "memory");
+  return v;
+}
+template <class R>
+__device__ __forceinline__ cplx<R> dsmem_ld(const cplx<R>* p, unsigned rank) {
+  return {dsmem_ld(&p->re, rank), dsmem_ld(&p->im, rank)};
+}
+
 // --------------------------------------------------------------- host side --
 #define MAK_CUDA_TRY(expr)                         \
   do {                                             \

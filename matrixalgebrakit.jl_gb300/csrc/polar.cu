@@ -78,6 +78,14 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
   __shared__ T srow[GJ_NB];
   __shared__ T dinv_s;
   __shared__ int pivs, pivq;
+  // cluster variant: this CTA's published pivot candidate, candidate row and
+  // (its holder) row jj, by column parity, read by the other CTAs through
+  // distributed shared memory after the cluster barrier
+  __shared__ R x_val[2];
+  __shared__ int x_idx[2];
+  __shared__ T x_cand[2][GJ_NB];
+  __shared__ T x_rowjj[2][GJ_NB];
+  constexpr bool kCl = SYNC == SYNC_CLUSTER;
   const int G = gridDim.x, cb = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
   const int rpc = a.rpc, b = a.b, k0 = a.k0;
@@ -118,7 +126,10 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
     }
     if (lane == 0) { sv[wid] = best; si[wid] = bidx; }
     if (jj >= r0 && jj < r0 + nr)
-      for (int c = tid; c < b; c += blockDim.x) rowjj[c] = Ps[(jj - r0) + c * rpc];
+      for (int c = tid; c < b; c += blockDim.x) {
+        if constexpr (kCl) x_rowjj[par][c] = Ps[(jj - r0) + c * rpc];
+        else rowjj[c] = Ps[(jj - r0) + c * rpc];
+      }
     __syncthreads();
     if (wid == 0) {
       R v = lane < nw ? sv[lane] : R(-1);
@@ -130,8 +141,13 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
         amax_merge(v, ix, v2, i2);
       }
       if (lane == 0) {
-        pval[cb] = v;
-        pidx[cb] = ix;
+        if constexpr (kCl) {
+          x_val[par] = v;
+          x_idx[par] = ix;
+        } else {
+          pval[cb] = v;
+          pidx[cb] = ix;
+        }
         pivs = ix;
       }
     }
@@ -139,8 +155,10 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
     {
       const int li = pivs;  // this CTA's candidate row (global index)
       if (li != INT_MAX)
-        for (int c = tid; c < b; c += blockDim.x)
-          cand[(int64_t)cb * GJ_NB + c] = Ps[(li - r0) + c * rpc];
+        for (int c = tid; c < b; c += blockDim.x) {
+          if constexpr (kCl) x_cand[par][c] = Ps[(li - r0) + c * rpc];
+          else cand[(int64_t)cb * GJ_NB + c] = Ps[(li - r0) + c * rpc];
+        }
     }
     if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
 
@@ -149,8 +167,15 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
       R v = R(-1);
       int ix = INT_MAX, iq = -1;
       for (int q = lane; q < G; q += 32) {
-        const R v2 = ld_cg(&pval[q]);
-        const int i2 = ld_cg(&pidx[q]);
+        R v2;
+        int i2;
+        if constexpr (kCl) {
+          v2 = dsmem_ld(&x_val[par], (unsigned)q);
+          i2 = dsmem_ld(&x_idx[par], (unsigned)q);
+        } else {
+          v2 = ld_cg(&pval[q]);
+          i2 = ld_cg(&pidx[q]);
+        }
         if (v2 > v || (v2 == v && i2 < ix)) { v = v2; ix = i2; iq = q; }
       }
 #pragma unroll
@@ -168,10 +193,20 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
     __syncthreads();
     const int p = pivs, q = pivq;
     // pivot row: the winning CTA's candidate (row jj itself when p == jj)
-    for (int c = tid; c < b; c += blockDim.x)
-      prow[c] = q < 0 ? ld_cg(&rowjj[c]) : ld_cg(&cand[(int64_t)q * GJ_NB + c]);
-    if (p != jj && p >= r0 && p < r0 + nr)
-      for (int c = tid; c < b; c += blockDim.x) Ps[(p - r0) + c * rpc] = ld_cg(&rowjj[c]);
+    if constexpr (kCl) {
+      const unsigned own = (unsigned)(jj / rpc);  // the CTA holding row jj
+      for (int c = tid; c < b; c += blockDim.x)
+        prow[c] = q < 0 ? dsmem_ld(&x_rowjj[par][c], own)
+                        : dsmem_ld(&x_cand[par][c], (unsigned)q);
+      if (p != jj && p >= r0 && p < r0 + nr)
+        for (int c = tid; c < b; c += blockDim.x)
+          Ps[(p - r0) + c * rpc] = dsmem_ld(&x_rowjj[par][c], own);
+    } else {
+      for (int c = tid; c < b; c += blockDim.x)
+        prow[c] = q < 0 ? ld_cg(&rowjj[c]) : ld_cg(&cand[(int64_t)q * GJ_NB + c]);
+      if (p != jj && p >= r0 && p < r0 + nr)
+        for (int c = tid; c < b; c += blockDim.x) Ps[(p - r0) + c * rpc] = ld_cg(&rowjj[c]);
+    }
     if (cb == 0 && tid == 0) a.piv[jj] = p;
     __syncthreads();
     if (tid == 0) {
@@ -202,6 +237,9 @@ __global__ void __launch_bounds__(GJ_THREADS) gje_panel_kernel(GjArgs<T> a) {
     }
     __syncthreads();
   }
+  // cluster variant: no CTA leaves (releasing its shared memory) while
+  // another may still read its last column's partials
+  if constexpr (kCl) panel_sync<SYNC>(a.bar, G, a.status);
   for (int c = 0; c < b; c++)
     for (int r = tid; r < nr; r += blockDim.x) Xp[(r0 + r) + (int64_t)c * a.ldx] = Ps[r + c * rpc];
 }
@@ -264,6 +302,9 @@ static size_t gj_slab_cap() {
     cudaFuncAttributes fa;
     size_t stat = 16 * 1024;
     if (cudaFuncGetAttributes(&fa, gje_panel_kernel<T, SYNC_GRID>) == cudaSuccess)
+      stat = fa.sharedSizeBytes;
+    if (cudaFuncGetAttributes(&fa, gje_panel_kernel<T, SYNC_CLUSTER>) == cudaSuccess &&
+        fa.sharedSizeBytes > stat)
       stat = fa.sharedSizeBytes;
     const size_t cap = (size_t)max_smem_optin() - stat - 1024;
     cudaFuncSetAttribute(gje_panel_kernel<T, SYNC_GRID>,

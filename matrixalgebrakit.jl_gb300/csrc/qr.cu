@@ -213,6 +213,13 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
   __shared__ T red_w[PANEL_THREADS / 32][NBMAX];
   __shared__ T sc[3];
   __shared__ T rowj[NBMAX];
+  // cluster variant: this CTA's published partials of the current column
+  // (by column parity), read by the other CTAs through distributed shared
+  // memory after the cluster barrier
+  __shared__ R x_nrm[2][2];      // sum of squares, largest magnitude
+  __shared__ T x_w[2][NBMAX];    // dot partials
+  __shared__ T x_row[2][NBMAX];  // row j (the CTA that holds it)
+  constexpr bool kCl = SYNC == SYNC_CLUSTER;
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
   const int rpc = a.rpc, jb = a.jb;
@@ -278,17 +285,28 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
       if (lane == j) red_k[wid] = mk;
     }
     if (j >= r0 && j < r0 + nr)
-      for (int c = j + tid; c < jb; c += blockDim.x) prow[c] = Ps[(j - r0) + c * ldp];
+      for (int c = j + tid; c < jb; c += blockDim.x) {
+        if constexpr (kCl) x_row[par][c] = Ps[(j - r0) + c * ldp];
+        else prow[c] = Ps[(j - r0) + c * ldp];
+      }
     __syncthreads();
     if (wid == 0) {
       T s = zero_<T>();
       for (int w = 0; w < nw; w++) s += red_w[w][lane];
-      if (lane > j && lane < jb) pw[(int64_t)b * NBMAX + lane] = s;
+      if (lane > j && lane < jb) {
+        if constexpr (kCl) x_w[par][lane] = s;
+        else pw[(int64_t)b * NBMAX + lane] = s;
+      }
       if (lane == j) {
         Key m = 0;
         for (int w = 0; w < nw; w++) m = red_k[w] > m ? red_k[w] : m;
-        pn[b] = re_(s);
-        pn[a.gstride + b] = NK::val(m);
+        if constexpr (kCl) {
+          x_nrm[par][0] = re_(s);
+          x_nrm[par][1] = NK::val(m);
+        } else {
+          pn[b] = re_(s);
+          pn[a.gstride + b] = NK::val(m);
+        }
       }
     }
     if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
@@ -301,9 +319,15 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
       R s = R(0);
       Key m = 0;
       for (int q = lane; q < G; q += 32) {
-        s += ld_cg(&pn[q]);
-        const Key k = NK::key(ld_cg(&pn[a.gstride + q]));
-        m = k > m ? k : m;
+        if constexpr (kCl) {
+          s += dsmem_ld(&x_nrm[par][0], (unsigned)q);
+          const Key k = NK::key(dsmem_ld(&x_nrm[par][1], (unsigned)q));
+          m = k > m ? k : m;
+        } else {
+          s += ld_cg(&pn[q]);
+          const Key k = NK::key(ld_cg(&pn[a.gstride + q]));
+          m = k > m ? k : m;
+        }
       }
       s = warp_sum(s);
       m = warp_max_key(m);
@@ -319,17 +343,25 @@ __global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T>
       T a0 = zero_<T>(), a1 = zero_<T>(), a2 = zero_<T>(), a3 = zero_<T>();
       if (lane > j && lane < jb) {
         int q = q0;
-        for (; q + 3 < q1; q += 4) {
-          a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
-          a1 += ld_cg(&pw[(int64_t)(q + 1) * NBMAX + lane]);
-          a2 += ld_cg(&pw[(int64_t)(q + 2) * NBMAX + lane]);
-          a3 += ld_cg(&pw[(int64_t)(q + 3) * NBMAX + lane]);
+        if constexpr (kCl) {
+          for (; q < q1; q++) a0 += dsmem_ld(&x_w[par][lane], (unsigned)q);
+        } else {
+          for (; q + 3 < q1; q += 4) {
+            a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
+            a1 += ld_cg(&pw[(int64_t)(q + 1) * NBMAX + lane]);
+            a2 += ld_cg(&pw[(int64_t)(q + 2) * NBMAX + lane]);
+            a3 += ld_cg(&pw[(int64_t)(q + 3) * NBMAX + lane]);
+          }
+          for (; q < q1; q++) a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
         }
-        for (; q < q1; q++) a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
       }
       red_w[wid][lane] = (a0 + a1) + (a2 + a3);
     }
-    if (wid == (nw > 1 ? 1 : 0) && lane >= j && lane < jb) rowj[lane] = ld_cg(&prow[lane]);
+    if (wid == (nw > 1 ? 1 : 0) && lane >= j && lane < jb) {
+      // row j is held by the CTA whose rows contain j
+      if constexpr (kCl) rowj[lane] = dsmem_ld(&x_row[par][lane], (unsigned)(j / rpc));
+      else rowj[lane] = ld_cg(&prow[lane]);
+    }
     __syncthreads();
     const bool rescale = sc_flag != 0;
     R xnorm = R(0);  // meaningful in thread 0 only (the scalars below)
@@ -720,6 +752,9 @@ static size_t panel_slab_cap() {
     cudaFuncAttributes fa;
     size_t stat = 48 * 1024;
     if (cudaFuncGetAttributes(&fa, qr_panel_kernel<T, SYNC_GRID>) == cudaSuccess)
+      stat = fa.sharedSizeBytes;
+    if (cudaFuncGetAttributes(&fa, qr_panel_kernel<T, SYNC_CLUSTER>) == cudaSuccess &&
+        fa.sharedSizeBytes > stat)
       stat = fa.sharedSizeBytes;
     const size_t cap = (size_t)max_smem_optin() - stat - 1024;
     cudaFuncSetAttribute(qr_panel_kernel<T, SYNC_GRID>,
