@@ -201,7 +201,8 @@ __device__ __forceinline__ void larfg_scalars_ssq(T alpha, real_t<T> ssq, real_t
 }
 
 template <class T, int SYNC>
-__global__ void __launch_bounds__(PANEL_THREADS, 1) qr_panel_kernel(PanelArgs<T> a) {
+__global__ void __launch_bounds__(PANEL_THREADS, SYNC == SYNC_CLUSTER ? 2 : 1)
+qr_panel_kernel(PanelArgs<T> a) {
   using R = real_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x jb, column-major, ld = ldp
@@ -859,7 +860,11 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8 &&
                      (traits<T>::cpx ? 4.0 : 1.0) * (double)m * (double)n * QR_OUTER_NB >=
                          split_min_mnk();
-  const int NBO = mixed ? QR_OUTER_NB : nb;
+  // outer block of the mixed path: 128 columns, or 64 for blocks whose
+  // columns number at most MAK_QR_OUTER64_MAX_N (default 0: never), where
+  // fewer 32-wide panels per block leave fewer within-block native updates
+  static const int outer64_max_n = (int)env_param("MAK_QR_OUTER64_MAX_N", 0, 0, 1 << 30);
+  const int NBO = mixed ? (n <= outer64_max_n ? 64 : QR_OUTER_NB) : nb;
   const int64_t nblk_o = ceil_div(k, NBO);
 
   T* tau = ar.take<T>(k > 0 ? k : 1);
