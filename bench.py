@@ -90,7 +90,7 @@ def parse():
     ap.add_argument("--no-pullback", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-tensors", type=int, default=256)
-    ap.add_argument("--workload", choices=["qr", "gemm", "polar", "batched", "sweep"],
+    ap.add_argument("--workload", choices=["qr", "gemm", "polar", "batched", "sweep", "autotune"],
                     default="qr",
                     help="gemm: time the split-precision product alone on --gemm-shapes; "
                          "polar: left_polar! alone on --polar-n; batched: the batch of "
@@ -1158,6 +1158,34 @@ def run_sweep_only(args):
     return 0
 
 
+def run_autotune(args):
+    """The autotuner of the drivers' tuning table on the batch of uneven
+    blocks (mixed precision, batched QR then batched polar, both replayed
+    from a CUDA graph); prints the table and every trial."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    mak = ge.load_package()
+    rng = np.random.default_rng(SEED + 11)
+    As = []
+    for i in range(args.batched_blocks):
+        m = int(rng.integers(8, 1025))
+        n = int(rng.integers(4, m + 1))
+        if i < args.batched_blocks // 2:
+            x = rng.standard_normal((n, m))
+        else:
+            x = rng.standard_normal((n, m)) + 1j * rng.standard_normal((n, m))
+        As.append(torch.from_numpy(x).to(dev).t())
+    res = mak.autotune.autotune_batched(As, precision="mixed",
+                                        kinds=tuple(args.batched_kinds.split(",")))
+    print(json.dumps(res), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1168,6 +1196,8 @@ def main():
         return run_batched_only(args)
     if args.workload == "sweep":
         return run_sweep_only(args)
+    if args.workload == "autotune":
+        return run_autotune(args)
     if args.workload == "polar":
         return run_polar_only(args)
     return run_gb300(args)

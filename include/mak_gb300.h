@@ -111,6 +111,33 @@ int mak_profile_start(void);
 int mak_profile_stop(void);
 int mak_profile_read(int kind, double* total_ms, double* total_work, uint64_t* launches);
 
+/* Tuning parameters of the drivers (no counterpart in the reference, whose
+ * drivers are LAPACK's / CUSOLVER's own): thresholds and counts that choose
+ * between code paths and launch shapes.  A parameter's value is the one set
+ * here, else the environment variable of the same name, else the built-in
+ * default (measured best on a GB300); it is read at every use, process wide,
+ * so set a table before the calls it should affect.  Names:
+ *   MAK_BATCH_STREAMS      internal streams of the batched calls (1..32, 32)
+ *   MAK_BATCH_GEMM_CTAS    CTA cap of each split product in a batched call
+ *                          (8..1024, a quarter of the SMs)
+ *   MAK_SIGN_FIXED_ITERS   Sylvester sign steps of the batched polar pullback
+ *                          (4..200, 30)
+ *   MAK_SPLIT_MIN_MNK      smallest product (multiply-adds, complex 4x) that
+ *                          takes the split tensor-core path (2^22)
+ *   MAK_GJ_SPLIT_MIN       n^2 128 (complex 4x) from which the mixed
+ *                          Gauss-Jordan inverse blocks by 128 (2^25)
+ *   MAK_NS_FIXED_MIN_N / MAK_NS_FIXED_MAX_N  n range of the Newton-Schulz
+ *                          finish in the batched polar (256 .. 2^30)
+ *   MAK_QR_OUTER64_MAX_N   mixed QR: 64-wide outer blocks up to this n (0)
+ *   MAK_LOOKAHEAD_CTAS     SMs of the look-ahead side stream (8..120, 48)
+ * mak_tuning_set: 0 ok, -1 unknown name, -2 value out of range; a NaN value
+ * returns the parameter to its environment / default value.
+ * mak_tuning_get: the value in effect.  mak_tuning_name(i): the i-th name,
+ * NULL past the last. */
+int mak_tuning_set(const char* name, double value);
+int mak_tuning_get(const char* name, double* value);
+const char* mak_tuning_name(int index);
+
 /* Self-test of the failure path of the bounded device-side waits (no
  * counterpart in the reference, whose waits are inside LAPACK / CUSOLVER).
  * Launches `ctas` co-resident CTAs that meet at the grid barrier the panel

@@ -69,3 +69,7 @@ __all__ += ["RightOrthViaLQ", "RightOrthViaPolar", "left_orth", "left_orth_", "r
 from . import autodiff  # noqa: E402  (torch.autograd front-end over the device pullbacks)
 
 __all__ += ["autodiff"]
+
+from . import autotune  # noqa: E402  (tuning table of the drivers and its autotuner)
+
+__all__ += ["autotune"]

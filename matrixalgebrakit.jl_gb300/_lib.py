@@ -124,6 +124,10 @@ for _s in "dzsc":
     SIGNATURES[f"mak_lq_pullback_{_s}"] = SIGNATURES[f"mak_qr_pullback_{_s}"]
 SIGNATURES["mak_right_polar_pushforward_workspace"] = (C.c_int, [C.c_int, _i64, _i64, C.c_int,
                                                                  C.POINTER(_sz)])
+# tuning table of the drivers
+SIGNATURES["mak_tuning_set"] = (C.c_int, [C.c_char_p, C.c_double])
+SIGNATURES["mak_tuning_get"] = (C.c_int, [C.c_char_p, C.POINTER(C.c_double)])
+SIGNATURES["mak_tuning_name"] = (C.c_char_p, [C.c_int])
 # self-test of the bounded device waits (failure path)
 SIGNATURES["mak_selftest_barrier"] = (C.c_int, [C.c_int, C.c_int, _i64, _p, _sz, _p, _p])
 

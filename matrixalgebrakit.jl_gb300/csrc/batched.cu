@@ -35,8 +35,7 @@ namespace mak {
 // better the more streams carry them.
 constexpr int kMaxBatchStreams = 32;
 static int batch_streams() {
-  static const int v = (int)env_param("MAK_BATCH_STREAMS", kMaxBatchStreams, 1, kMaxBatchStreams);
-  return v;
+  return (int)tuning(TUNE_BATCH_STREAMS);
 }
 
 struct StreamPool {
@@ -182,8 +181,7 @@ static int batched(int kind, const mak_batch_item* items, int nitems, const void
     // the batch's streams already overlap the blocks (no look-ahead), and a
     // quarter of the SMs per split product lets several blocks' persistent
     // tensor-core grids and native kernels share the GPU
-    static const int budget = (int)env_param("MAK_BATCH_GEMM_CTAS", num_sms() / 4, 8, 1024);
-    ThreadSettingsScope settings(false, budget);
+    ThreadSettingsScope settings(false, (int)tuning(TUNE_BATCH_GEMM_CTAS));
     for (int i : order) {
       const int s = p.owner[i];
       Arena ar((char*)work + p.off[s], p.ws_stream[s]);
@@ -221,8 +219,7 @@ static int batched_ws(int kind, const mak_batch_item* items, int nitems, const v
 enum { BATCH_QR_PB = 2, BATCH_POLAR_PB = 3 };
 
 static int sign_fixed_iters() {
-  static const int v = (int)env_param("MAK_SIGN_FIXED_ITERS", 30, 4, 200);
-  return v;
+  return (int)tuning(TUNE_SIGN_FIXED_ITERS);
 }
 
 template <class T>
@@ -367,7 +364,7 @@ static int batched_pb(int kind, const mak_batch_pullback_item* items, int nitems
   };
   std::vector<int> known(nitems, -1);
   int rc_all = 0;
-  ThreadSettingsScope settings(false, (int)env_param("MAK_BATCH_GEMM_CTAS", num_sms() / 4, 8, 1024));
+  ThreadSettingsScope settings(false, (int)tuning(TUNE_BATCH_GEMM_CTAS));
   if (kind == BATCH_QR_PB) {
     // every block's rank, then one read of them all
     MAK_TRY(fork());

@@ -9,18 +9,7 @@
 
 namespace mak {
 
-double split_min_mnk() {
-  static double v = 4194304.0;  // 2^22
-  static std::once_flag f;
-  std::call_once(f, [] {
-    const char* e = getenv("MAK_SPLIT_MIN_MNK");
-    if (e && *e) {
-      const double x = atof(e);
-      if (x >= 1.0 && x <= 1e15) v = x;
-    }
-  });
-  return v;
-}
+double split_min_mnk() { return tuning(TUNE_SPLIT_MIN_MNK); }
 
 // C = alpha * sum_s part[s] + beta * C  (fixed summation order)
 template <class T>

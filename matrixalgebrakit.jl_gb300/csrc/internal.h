@@ -43,17 +43,23 @@ int polar_pullback_run(cudaStream_t st, int64_t m, int64_t n, T* dA, int64_t ldd
                        const T* dP, int64_t lddp, int maxiter, int precision, Arena& ar,
                        mak_info* info);
 
-// A numeric tuning parameter: the environment variable `name` when it is set
-// and within [lo, hi], else `dflt`.  Call sites keep the value in a
-// function-local static, so it is read once per process.
-inline double env_param(const char* name, double dflt, double lo, double hi) {
-  const char* e = getenv(name);
-  if (e && *e) {
-    const double x = atof(e);
-    if (x >= lo && x <= hi) return x;
-  }
-  return dflt;
-}
+// Tuning parameters of the drivers (tuning.cu): the value set through
+// mak_tuning_set, else the environment variable of the same name, else the
+// built-in default.  Read at every use, so a table loaded by the caller
+// takes effect for the calls that follow.
+enum TuneId {
+  TUNE_BATCH_STREAMS = 0,    // internal streams of the batched calls
+  TUNE_BATCH_GEMM_CTAS,      // per-product CTA cap inside a batched call
+  TUNE_SIGN_FIXED_ITERS,     // sign-iteration steps of the batched polar pullback
+  TUNE_SPLIT_MIN_MNK,        // smallest product (multiply-adds) taking the split path
+  TUNE_GJ_SPLIT_MIN,         // n^2 128 from which Gauss-Jordan blocks by 128 (mixed)
+  TUNE_NS_FIXED_MIN_N,       // Newton-Schulz finish in the batched polar: n range
+  TUNE_NS_FIXED_MAX_N,
+  TUNE_QR_OUTER64_MAX_N,     // mixed QR: 64-wide outer blocks up to this n
+  TUNE_LOOKAHEAD_CTAS,       // SMs of the look-ahead side stream
+  TUNE_COUNT
+};
+double tuning(int id);
 
 // Look-ahead (QR and Gauss-Jordan): a high-priority side stream factors the
 // next block while the main stream updates the far columns.  On/off for

@@ -332,7 +332,7 @@ int gje_inverse(cudaStream_t st, int64_t n, T* X, int64_t ldx, int* iperm, int p
   // replay, 16 streams): gate 2^29 / 2^25 / 2^23 gave 2.23 / 1.80 / 1.75 s;
   // the launches the lower gates add only cost when they are not replayed
   // from a graph (the same batch issued eagerly: 2.68 / 5.47 / 5.64 s).
-  static const double gate = env_param("MAK_GJ_SPLIT_MIN", 33554432.0 /* 2^25 */, 1.0, 1e18);
+  const double gate = tuning(TUNE_GJ_SPLIT_MIN);
   const bool mixed = precision == MAK_PREC_MIXED && sizeof(real_t<T>) == 8 &&
                      (traits<T>::cpx ? 4.0 : 1.0) * (double)n * (double)n * GJ_OUTER_NB >= gate;
   const int NBO = mixed ? GJ_OUTER_NB : GJ_NB;
@@ -651,8 +651,7 @@ int polar_newton_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T
   // 256 <= n <= 384 only 1.80 s, for every n >= 256 1.54 s.  The
   // host-checked loop launches just the step it takes and uses the finish
   // at every n.
-  static const int ns_lo = (int)env_param("MAK_NS_FIXED_MIN_N", 256, 0, 1 << 30);
-  static const int ns_hi = (int)env_param("MAK_NS_FIXED_MAX_N", 1 << 30, 0, 1 << 30);
+  const double ns_lo = tuning(TUNE_NS_FIXED_MIN_N), ns_hi = tuning(TUNE_NS_FIXED_MAX_N);
   const bool ns_fixed_ok = ns_ok && n >= ns_lo && n <= ns_hi;
   T* Qw = (m > n) ? ar.take<T>((size_t)m * n) : nullptr;
   T* Rw = (m > n) ? ar.take<T>((size_t)n * n) : nullptr;

@@ -583,18 +583,7 @@ constexpr int QR_OUTER_NB = 128;  // outer block of the mixed-precision path
 // SMs given to the look-ahead side stream (panels and the block Gram) while
 // the main stream's persistent tensor-core grid takes the rest; 48 by
 // default, MAK_LOOKAHEAD_CTAS overrides it (read once, clamped to 8..120).
-int lookahead_ctas() {
-  static int v = 48;
-  static std::once_flag f;
-  std::call_once(f, [] {
-    const char* e = getenv("MAK_LOOKAHEAD_CTAS");
-    if (e && *e) {
-      const int x = atoi(e);
-      v = x < 8 ? 8 : (x > 120 ? 120 : x);
-    }
-  });
-  return v;
-}
+int lookahead_ctas() { return (int)tuning(TUNE_LOOKAHEAD_CTAS); }
 
 static thread_local bool tl_no_lookahead = false;
 bool lookahead_enabled() { return !tl_no_lookahead; }
@@ -863,8 +852,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   // outer block of the mixed path: 128 columns, or 64 for blocks whose
   // columns number at most MAK_QR_OUTER64_MAX_N (default 0: never), where
   // fewer 32-wide panels per block leave fewer within-block native updates
-  static const int outer64_max_n = (int)env_param("MAK_QR_OUTER64_MAX_N", 0, 0, 1 << 30);
-  const int NBO = mixed ? (n <= outer64_max_n ? 64 : QR_OUTER_NB) : nb;
+  const int NBO = mixed ? ((double)n <= tuning(TUNE_QR_OUTER64_MAX_N) ? 64 : QR_OUTER_NB) : nb;
   const int64_t nblk_o = ceil_div(k, NBO);
 
   T* tau = ar.take<T>(k > 0 ? k : 1);

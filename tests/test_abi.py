@@ -209,3 +209,42 @@ def test_every_entry_point_refuses_host_tensors(mak):
     for call in calls:
         with pytest.raises(mak.ArgumentError, match="CUDA device"):
             call()
+
+
+def test_tuning_table_is_host_only(mak):
+    """The drivers' tuning table: every parameter has a value without a GPU,
+    setting checks the name and the range, NaN returns to the default."""
+    import math
+
+    from mak_gb300 import autotune
+
+    names = autotune.tuning_names()
+    assert "MAK_BATCH_STREAMS" in names and "MAK_SPLIT_MIN_MNK" in names
+    before = autotune.get_tuning()
+    assert set(before) == set(names)
+    autotune.set_tuning(MAK_BATCH_STREAMS=8, MAK_SPLIT_MIN_MNK=2.0 ** 20)
+    assert autotune.get_tuning("MAK_BATCH_STREAMS") == 8
+    assert autotune.get_tuning("MAK_SPLIT_MIN_MNK") == 2.0 ** 20
+    with pytest.raises(ValueError):
+        autotune.set_tuning(MAK_BATCH_STREAMS=64)
+    with pytest.raises(KeyError):
+        autotune.set_tuning(MAK_NO_SUCH_PARAMETER=1)
+    autotune.reset_tuning()
+    assert autotune.get_tuning() == before
+    lib = mak.library()
+    assert lib.mak_tuning_set(b"MAK_BATCH_STREAMS", math.nan) == 0
+    assert lib.mak_tuning_name(len(names)) is None
+
+
+def test_tuning_table_json_round_trip(mak, tmp_path):
+    from mak_gb300 import autotune
+
+    path = tmp_path / "tune.json"
+    autotune.save_tuning({"table": {"MAK_BATCH_STREAMS": 16, "MAK_GJ_SPLIT_MIN": 2.0 ** 27}},
+                         path)
+    autotune.load_tuning(path, strict=False)
+    try:
+        assert autotune.get_tuning("MAK_BATCH_STREAMS") == 16
+        assert autotune.get_tuning("MAK_GJ_SPLIT_MIN") == 2.0 ** 27
+    finally:
+        autotune.reset_tuning()
