@@ -57,6 +57,7 @@ enum TuneId {
   TUNE_NS_FIXED_MAX_N,
   TUNE_QR_OUTER64_MAX_N,     // mixed QR: 64-wide outer blocks up to this n
   TUNE_LOOKAHEAD_CTAS,       // SMs of the look-ahead side stream
+  TUNE_PANEL_HIER_C,         // tall panels: cooperative grid of clusters of this size (0: off)
   TUNE_COUNT
 };
 double tuning(int id);

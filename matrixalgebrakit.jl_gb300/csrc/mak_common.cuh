@@ -291,13 +291,54 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, in
 // take the same branches in every CTA, so every thread of the cluster
 // arrives.  Unlike a cooperative launch, cluster launches of different
 // streams run side by side.
-enum { SYNC_GRID = 0, SYNC_CLUSTER = 1 };
+//
+// SYNC_HIER: a cooperative grid made of clusters (launched with both the
+// cooperative and the cluster attribute).  The CTAs of a cluster meet at
+// the cluster barrier and only the clusters' first CTAs meet at the bounded
+// global barrier (`nblocks` = the number of clusters), then release their
+// clusters with a second cluster barrier: far fewer arrivals on the global
+// counter, and the panels can combine a cluster's partials through
+// distributed shared memory before the global round.  On a timeout every
+// CTA of a cluster learns it from its cluster's flag after the last cluster
+// barrier (no CTA is left waiting at a cluster barrier).
+enum { SYNC_GRID = 0, SYNC_CLUSTER = 1, SYNC_HIER = 2 };
+__device__ __forceinline__ unsigned cluster_ctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_nctarank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+// the second half of a SYNC_HIER barrier: the clusters' first CTAs meet at
+// the global barrier, record its outcome in their cluster's flag and
+// release their clusters; every CTA of a cluster then reads the same flag,
+// so a cluster always takes one branch (a CTA that left while the others
+// went on to the next cluster barrier would leave them waiting for good)
+__device__ __forceinline__ bool hier_leader_barrier(unsigned* bar, unsigned nclusters, int* status,
+                                                    int* cluster_flag) {
+  if (cluster_ctarank() == 0) {
+    const bool ok = grid_barrier(bar, nclusters, status);
+    if (threadIdx.x == 0) *(volatile int*)cluster_flag = ok ? 1 : 0;
+  }
+  cluster_sync_all();
+  return __ldcg(cluster_flag) != 0;
+}
 template <int SYNC>
-__device__ __forceinline__ bool panel_sync(unsigned* bar, unsigned nblocks, int* status) {
+__device__ __forceinline__ bool panel_sync(unsigned* bar, unsigned nblocks, int* status,
+                                           int* cluster_flag = nullptr) {
   if constexpr (SYNC == SYNC_CLUSTER) {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
-                     : "memory");
+    cluster_sync_all();
     return true;
+  } else if constexpr (SYNC == SYNC_HIER) {
+    cluster_sync_all();
+    return hier_leader_barrier(bar, nblocks, status, cluster_flag);
   } else {
     return grid_barrier(bar, nblocks, status);
   }

@@ -60,6 +60,7 @@ struct PanelArgs {
   T* alpha_buf;         // [2][NBMAX]: row j of the panel by column parity
   T* gram;              // [NBMAX*NBMAX]: the panel's reduced Gram matrix V^H V
   unsigned* bar;        // grid barrier words
+  int* cflag;           // [gstride] outcome of the last global round, per cluster (SYNC_HIER)
   int* status;
   int gstride;          // allocation stride of the per-CTA partial rows
 };
@@ -221,7 +222,15 @@ qr_panel_kernel(PanelArgs<T> a) {
   __shared__ T x_w[2][NBMAX];    // dot partials
   __shared__ T x_row[2][NBMAX];  // row j (the CTA that holds it)
   constexpr bool kCl = SYNC == SYNC_CLUSTER;
+  constexpr bool kH = SYNC == SYNC_HIER;
+  constexpr bool kSm = kCl || kH;  // partials published in shared memory first
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+  // hierarchical grid: C CTAs per cluster, H clusters; the global round
+  // then carries one partial row per cluster
+  const int C = kH ? (int)cluster_nctarank() : 1;
+  const int H = G / C;
+  const unsigned nsync = kH ? (unsigned)H : (unsigned)G;
+  int* const cflag = kH ? a.cflag + b / C : nullptr;
   const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
   const int rpc = a.rpc, jb = a.jb;
   const int ldp = rpc | 1;  // slab leading dimension (odd: conflict-free column strides)
@@ -287,7 +296,7 @@ qr_panel_kernel(PanelArgs<T> a) {
     }
     if (j >= r0 && j < r0 + nr)
       for (int c = j + tid; c < jb; c += blockDim.x) {
-        if constexpr (kCl) x_row[par][c] = Ps[(j - r0) + c * ldp];
+        if constexpr (kSm) x_row[par][c] = Ps[(j - r0) + c * ldp];
         else prow[c] = Ps[(j - r0) + c * ldp];
       }
     __syncthreads();
@@ -295,13 +304,13 @@ qr_panel_kernel(PanelArgs<T> a) {
       T s = zero_<T>();
       for (int w = 0; w < nw; w++) s += red_w[w][lane];
       if (lane > j && lane < jb) {
-        if constexpr (kCl) x_w[par][lane] = s;
+        if constexpr (kSm) x_w[par][lane] = s;
         else pw[(int64_t)b * NBMAX + lane] = s;
       }
       if (lane == j) {
         Key m = 0;
         for (int w = 0; w < nw; w++) m = red_k[w] > m ? red_k[w] : m;
-        if constexpr (kCl) {
+        if constexpr (kSm) {
           x_nrm[par][0] = re_(s);
           x_nrm[par][1] = NK::val(m);
         } else {
@@ -310,16 +319,48 @@ qr_panel_kernel(PanelArgs<T> a) {
         }
       }
     }
-    if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
+    if constexpr (kH) {
+      // the cluster's first CTA combines its C CTAs' partials (rank order)
+      // and publishes one row per cluster for the global round
+      cluster_sync_all();
+      if (cluster_ctarank() == 0) {
+        const int h = b / C;
+        if (wid == 0) {
+          if (lane == j) {
+            R s2 = R(0);
+            Key m2 = 0;
+            for (int r = 0; r < C; r++) {
+              s2 += dsmem_ld(&x_nrm[par][0], (unsigned)r);
+              const Key k = NK::key(dsmem_ld(&x_nrm[par][1], (unsigned)r));
+              m2 = k > m2 ? k : m2;
+            }
+            pn[h] = s2;
+            pn[a.gstride + h] = NK::val(m2);
+          }
+          if (lane > j && lane < jb) {
+            T s2 = zero_<T>();
+            for (int r = 0; r < C; r++) s2 += dsmem_ld(&x_w[par][lane], (unsigned)r);
+            pw[(int64_t)h * NBMAX + lane] = s2;
+          }
+        }
+        const int own = j / rpc;  // the CTA holding row j
+        if (own / C == h && wid == 1 && lane >= j && lane < jb)
+          prow[lane] = dsmem_ld(&x_row[par][lane], (unsigned)(own % C));
+      }
+      if (!hier_leader_barrier(a.bar, nsync, a.status, cflag)) return;
+    } else {
+      if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
+    }
 
     // ---- phase B: every CTA combines the partials in the same fixed order
     // and so derives bit-identical beta / tau / w.  Warp 0: the norm; every
     // warp: a slice of the CTAs' dot partials (lane = column); lane j of
     // warp 1 (or of warp 0 with one warp): row j.
+    const int NP = kH ? H : G;  // partial rows to combine
     if (wid == 0) {
       R s = R(0);
       Key m = 0;
-      for (int q = lane; q < G; q += 32) {
+      for (int q = lane; q < NP; q += 32) {
         if constexpr (kCl) {
           s += dsmem_ld(&x_nrm[par][0], (unsigned)q);
           const Key k = NK::key(dsmem_ld(&x_nrm[par][1], (unsigned)q));
@@ -339,8 +380,8 @@ qr_panel_kernel(PanelArgs<T> a) {
       }
     }
     {
-      const int per = (G + nw - 1) / nw;
-      const int q0 = wid * per, q1 = min(G, q0 + per);
+      const int per = (NP + nw - 1) / nw;
+      const int q0 = wid * per, q1 = min(NP, q0 + per);
       T a0 = zero_<T>(), a1 = zero_<T>(), a2 = zero_<T>(), a3 = zero_<T>();
       if (lane > j && lane < jb) {
         int q = q0;
@@ -377,7 +418,7 @@ qr_panel_kernel(PanelArgs<T> a) {
       for (int r = rs + tid; r < nr; r += blockDim.x) ssq_scaled_add(ss2, col[r], scale);
       ss2 = block_sum(ss2, red_r);
       if (tid == 0) a.part_nrm[6 * a.gstride + b] = ss2;
-      if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
+      if (!panel_sync<SYNC>(a.bar, nsync, a.status, cflag)) return;
       if (wid == 0) {
         R s2 = R(0);
         for (int q = lane; q < G; q += 32) s2 += ld_cg(&a.part_nrm[6 * a.gstride + q]);
@@ -426,7 +467,7 @@ qr_panel_kernel(PanelArgs<T> a) {
         s = warp_sum(s);
         if (lane == 0) pw2[(int64_t)b * NBMAX + c] = s;
       }
-      if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
+      if (!panel_sync<SYNC>(a.bar, nsync, a.status, cflag)) return;
       {
         const int per = (G + nw - 1) / nw;
         const int q0 = wid * per, q1 = min(G, q0 + per);
@@ -488,7 +529,7 @@ qr_panel_kernel(PanelArgs<T> a) {
   }
   for (int c = 0; c < jb; c++)
     for (int r = tid; r < nr; r += blockDim.x) a.A[(r0 + r) + (int64_t)c * a.lda] = Ps[r + c * ldp];
-  if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
+  if (!panel_sync<SYNC>(a.bar, nsync, a.status, cflag)) return;
 
   // ---- reduce the Gram over the CTAs: one thread per pair, the CTAs'
   // partials in a fixed order (four interleaved accumulators)
@@ -510,7 +551,7 @@ qr_panel_kernel(PanelArgs<T> a) {
     for (; q < G; q++) s0 += ld_cg(src + q * NN);
     a.gram[i + jj * NBMAX] = (s0 + s1) + (s2 + s3);
   }
-  if (!panel_sync<SYNC>(a.bar, G, a.status)) return;
+  if (!panel_sync<SYNC>(a.bar, nsync, a.status, cflag)) return;
 
   // ---- T factor (larft, forward, column-wise): T = U^{-1} with U_ii =
   // 1/tau_i and U_il = G_il (i < l), each column an independent back
@@ -751,6 +792,8 @@ static size_t panel_slab_cap() {
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
     cudaFuncSetAttribute(qr_panel_kernel<T, SYNC_CLUSTER>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
+    cudaFuncSetAttribute(qr_panel_kernel<T, SYNC_HIER>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
     return cap;
   });
 }
@@ -767,6 +810,7 @@ constexpr int PANEL_CLUSTER_ROWS = 256;
 // above by the shared-memory slab size; at most one CTA per SM.
 struct PanelShape {
   int G, rpc, sync;
+  int cl = 1;  // CTAs per cluster (SYNC_CLUSTER: G; SYNC_HIER: the cluster size)
   size_t smem;
 };
 template <class T>
@@ -786,6 +830,7 @@ static int panel_shape(int64_t mp, int jb, PanelShape& ps, int want_ctas) {
     ps.G = (int)G;
     ps.rpc = (int)rpc;
     ps.sync = SYNC_CLUSTER;
+    ps.cl = (int)G;
     ps.smem = (size_t)(ps.rpc | 1) * jb * sizeof(T);
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
@@ -805,6 +850,41 @@ static int panel_shape(int64_t mp, int jb, PanelShape& ps, int want_ctas) {
       return 0;
     (void)cudaGetLastError();  // fall through to the cooperative grid
   }
+  // taller panels: a cooperative grid of clusters of C CTAs when the tuning
+  // table asks for it (MAK_PANEL_HIER_C), else a plain cooperative grid
+  const int hc = (int)tuning(TUNE_PANEL_HIER_C);
+  if (hc == 2 || hc == 4 || hc == 8) {
+    int64_t H = ceil_div(ceil_div(mp, 64), hc);
+    if (H * hc > want_ctas) H = want_ctas / hc;
+    if (H * hc > max_ctas) H = max_ctas / hc;
+    if (H >= 1) {
+      int64_t rpc = ceil_div(mp, H * hc);
+      if (rpc <= rpc_max) {
+        ps.G = (int)(H * hc);
+        ps.rpc = (int)rpc;
+        ps.sync = SYNC_HIER;
+        ps.cl = hc;
+        ps.smem = (size_t)(ps.rpc | 1) * jb * sizeof(T);
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        cfg.gridDim = dim3((unsigned)ps.G);
+        cfg.blockDim = dim3(PANEL_THREADS);
+        cfg.dynamicSmemBytes = ps.smem;
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)hc;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_kernel<T, SYNC_HIER>, &cfg) ==
+                cudaSuccess &&
+            nclusters >= H)
+          return 0;
+        (void)cudaGetLastError();
+      }
+    }
+  }
   int64_t G = ceil_div(mp, 64);
   if (G > want_ctas) G = want_ctas;
   if (G > max_ctas) G = max_ctas;
@@ -821,6 +901,7 @@ static int panel_shape(int64_t mp, int jb, PanelShape& ps, int want_ctas) {
   ps.G = (int)G;
   ps.rpc = (int)rpc;
   ps.sync = SYNC_GRID;
+  ps.cl = 1;
   ps.smem = (size_t)(ps.rpc | 1) * jb * sizeof(T);
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, qr_panel_kernel<T, SYNC_GRID>,
@@ -868,6 +949,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   T* alpha_buf = ar.take<T>(2 * NBMAX);  // row j of the panel, by column parity
   T* gram_buf = ar.take<T>((size_t)NBMAX * NBMAX);
   unsigned* bar = ar.take<unsigned>(2);
+  int* cflag = ar.take<int>(gmax);
   T *To = nullptr, *Gm = nullptr, *Wm = nullptr, *W2m = nullptr;
   char* ozs = nullptr;
   size_t oz_bytes = 0;
@@ -954,23 +1036,28 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     MAK_TRY(panel_shape<T>(mp, jb, ps, s == st ? sms : lookahead_ctas()));
     PanelArgs<T> pa{A + j0 + j0 * lda, lda, (int)mp, jb, ps.rpc, tau + j0,
                     Ts + (j0 / nb) * NBMAX * NBMAX, part_nrm, part_w, part_g, alpha_buf,
-                    gram_buf, bar, status, gmax};
+                    gram_buf, bar, cflag, status, gmax};
     ProfScope prof(s, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
     note_launch();
-    if (ps.sync == SYNC_CLUSTER) {
+    if (ps.sync == SYNC_CLUSTER || ps.sync == SYNC_HIER) {
       cudaLaunchConfig_t cfg = {};
-      cudaLaunchAttribute attr[1];
+      cudaLaunchAttribute attr[2];
       cfg.gridDim = dim3((unsigned)ps.G);
       cfg.blockDim = dim3(PANEL_THREADS);
       cfg.dynamicSmemBytes = ps.smem;
       cfg.stream = s;
       attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = (unsigned)ps.G;
+      attr[0].val.clusterDim.x = (unsigned)ps.cl;
       attr[0].val.clusterDim.y = 1;
       attr[0].val.clusterDim.z = 1;
+      attr[1].id = cudaLaunchAttributeCooperative;
+      attr[1].val.cooperative = 1;
       cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      MAK_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_kernel<T, SYNC_CLUSTER>, pa));
+      cfg.numAttrs = ps.sync == SYNC_HIER ? 2 : 1;
+      if (ps.sync == SYNC_HIER)
+        MAK_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_kernel<T, SYNC_HIER>, pa));
+      else
+        MAK_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_kernel<T, SYNC_CLUSTER>, pa));
       return 0;
     }
     void* args[] = {&pa};
