@@ -130,6 +130,11 @@ int mak_profile_read(int kind, double* total_ms, double* total_work, uint64_t* l
  *                          finish in the batched polar (256 .. 2^30)
  *   MAK_QR_OUTER64_MAX_N   mixed QR: 64-wide outer blocks up to this n (0)
  *   MAK_LOOKAHEAD_CTAS     SMs of the look-ahead side stream (8..120, 48)
+ *   MAK_PANEL_HIER_C       QR panels too tall for one cluster: 0 = one grid
+ *                          barrier over all panel CTAs; 2, 4 or 8 = clusters
+ *                          of that many CTAs combine through distributed
+ *                          shared memory and only their leaders meet at the
+ *                          grid barrier (0)
  * mak_tuning_set: 0 ok, -1 unknown name, -2 value out of range; a NaN value
  * returns the parameter to its environment / default value.
  * mak_tuning_get: the value in effect.  mak_tuning_name(i): the i-th name,
