@@ -58,6 +58,7 @@ enum TuneId {
   TUNE_QR_OUTER64_MAX_N,     // mixed QR: 64-wide outer blocks up to this n
   TUNE_LOOKAHEAD_CTAS,       // SMs of the look-ahead side stream
   TUNE_PANEL_HIER_C,         // tall panels: cooperative grid of clusters of this size (0: off)
+  TUNE_PANEL_PAIR,           // QR panels: two columns per barrier round (1) or one (0)
   TUNE_COUNT
 };
 double tuning(int id);

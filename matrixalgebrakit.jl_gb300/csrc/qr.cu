@@ -52,17 +52,20 @@ struct PanelArgs {
   int rpc;              // panel rows owned by one CTA
   T* tau;               // [jb]
   T* Tm;                // [NBMAX x NBMAX], ld NBMAX
-  real_t<T>* part_nrm;  // [2][3][gstride] by column parity (sums of squares, largest
-                        // magnitudes, spare), then [gstride] rescaled sums
-  T* part_w;            // [2][gstride][NBMAX] dot partials by column parity, then
-                        // [gstride][NBMAX] for the rescaled path
+  real_t<T>* part_nrm;  // [2][3][gstride] by round parity (sums of squares, largest
+                        // magnitudes of columns j and j+1), then [gstride] rescaled sums
+  T* part_w;            // [2][gstride][NBMAX] dot partials by round parity, then
+                        // [gstride][NBMAX] for the rescaled path, then
+                        // [2][gstride][NBMAX] column j+1's dot partials (pair rounds)
   T* part_g;            // [G][NBMAX*NBMAX]
-  T* alpha_buf;         // [2][NBMAX]: row j of the panel by column parity
+  T* alpha_buf;         // [2][NBMAX]: row j of the panel by round parity, then
+                        // [2][NBMAX] row j+1 (pair rounds)
   T* gram;              // [NBMAX*NBMAX]: the panel's reduced Gram matrix V^H V
   unsigned* bar;        // grid barrier words
   int* cflag;           // [gstride] outcome of the last global round, per cluster (SYNC_HIER)
   int* status;
   int gstride;          // allocation stride of the per-CTA partial rows
+  int pair;             // two columns per barrier round where the norms allow
 };
 
 // Column norms in the panel: a plain sum of squares (one FMA per element on
@@ -92,6 +95,11 @@ template <class R> __device__ __forceinline__ typename NormKey<R>::K mag_key(R x
 template <class R> __device__ __forceinline__ typename NormKey<R>::K mag_key(cplx<R> x) {
   const auto a = NormKey<R>::key(x.re), b = NormKey<R>::key(x.im);
   return a > b ? a : b;
+}
+__device__ __forceinline__ bool finite_(double x) { return isfinite(x); }
+__device__ __forceinline__ bool finite_(float x) { return isfinite(x); }
+template <class R> __device__ __forceinline__ bool finite_(cplx<R> x) {
+  return isfinite(x.re) && isfinite(x.im);
 }
 template <class R> __device__ __forceinline__ R sq_add(R s, R x) { return fma_(x, x, s); }
 template <class R> __device__ __forceinline__ R sq_add(R s, cplx<R> x) {
@@ -209,18 +217,22 @@ qr_panel_kernel(PanelArgs<T> a) {
   T* Ps = reinterpret_cast<T*>(smem_raw);  // rpc x jb, column-major, ld = ldp
   __shared__ R red_r[32];
   __shared__ typename NormKey<R>::K red_k[32];
+  __shared__ typename NormKey<R>::K red_k2[32];
   __shared__ R sc_r[3];
-  __shared__ int sc_flag;
-  __shared__ T wsh[NBMAX];
+  __shared__ int sc_flag, sc_flag2, sc_pair;
+  __shared__ T wsh[NBMAX], wsh1[NBMAX];
   __shared__ T red_w[PANEL_THREADS / 32][NBMAX];
-  __shared__ T sc[3];
-  __shared__ T rowj[NBMAX];
+  __shared__ T red_g[PANEL_THREADS / 32][NBMAX];  // pair rounds: column j+1's dots
+  __shared__ T sc[3], sc1[3];
+  __shared__ T rowj[NBMAX], rowj1[NBMAX];
   // cluster variant: this CTA's published partials of the current column
   // (by column parity), read by the other CTAs through distributed shared
   // memory after the cluster barrier
-  __shared__ R x_nrm[2][2];      // sum of squares, largest magnitude
-  __shared__ T x_w[2][NBMAX];    // dot partials
-  __shared__ T x_row[2][NBMAX];  // row j (the CTA that holds it)
+  __shared__ R x_nrm[2][3];       // sum of squares, largest magnitude (of column j+1 too)
+  __shared__ T x_w[2][NBMAX];     // dot partials
+  __shared__ T x_g[2][NBMAX];     // pair rounds: column j+1's dot partials
+  __shared__ T x_row[2][NBMAX];   // row j (the CTA that holds it)
+  __shared__ T x_row1[2][NBMAX];  // pair rounds: row j+1
   constexpr bool kCl = SYNC == SYNC_CLUSTER;
   constexpr bool kH = SYNC == SYNC_HIER;
   constexpr bool kSm = kCl || kH;  // partials published in shared memory first
@@ -251,53 +263,109 @@ qr_panel_kernel(PanelArgs<T> a) {
   // after every CTA passed barrier j, i.e. finished reading column j-1's.
   // A column whose largest magnitude lies outside [2^lo, 2^hi] takes the
   // rescaled two-round path instead (the same decision in every CTA).
-  for (int j = 0; j < jb; j++) {
+  // Pair rounds (pair_mode): one round publishes, next to column j's
+  // partials, the dot products of column j+1 below row j+1 with the columns
+  // c > j and row j+1.  Since H_j is unitary, column j+1's sum of squares
+  // and dot products after the reflection follow from those Gram entries,
+  // H_j's scalars and rows j, j+1, so column j+1's reflector is formed in
+  // the same round (a rank-2 update follows).  When that derivation would
+  // cancel (column j+1 keeps less than half of its norm below row j+1) or
+  // a magnitude is outside the safe range, column j+1 takes its own round
+  // instead; the test sees the same numbers in every CTA.
+  const bool pair_mode = !kH && a.pair != 0;
+  for (int j = 0, rnd = 0; j < jb; rnd++) {
     T* col = Ps + j * ldp;
-    const int par = j & 1;
+    T* col1 = col + ldp;  // column j+1 (pair rounds)
+    const int par = rnd & 1;
+    const bool two = pair_mode && j + 1 < jb;
     R* pn = a.part_nrm + (int64_t)par * 3 * a.gstride;
     T* pw = a.part_w + (int64_t)par * a.gstride * NBMAX;
+    T* pwg = a.part_w + (int64_t)(3 + par) * a.gstride * NBMAX;
     T* prow = a.alpha_buf + par * NBMAX;
+    T* prow1 = a.alpha_buf + (2 + par) * NBMAX;
     using NK = NormKey<R>;
     using Key = typename NK::K;
     const int rs = max(0, j + 1 - r0);  // first local row below the diagonal
+    const int jy = j + 1 - r0;          // local index of row j+1
     // ---- phase A: warp w takes a slice of this CTA's rows below the
     // diagonal; lane c >= j accumulates conj(x_r) A[r, c] over the slice
     // (lane j: conj(x_r) x_r, the sum of squares) and the largest magnitude
-    // of x.  No cross-lane reductions (GB300 issues about two FP64
-    // operations per clock per SM, so butterflies over 32 lanes would cost
-    // more than the products); warp 0 adds the eight slices.  The slab's
-    // odd leading dimension keeps the column-strided reads conflict-free.
+    // of x (pair rounds: also conj(y_r) A[r, c] for y = column j+1 below row
+    // j+1, and y's largest magnitude).  No cross-lane reductions (GB300
+    // issues about two FP64 operations per clock per SM, so butterflies over
+    // 32 lanes would cost more than the products); warp 0 adds the eight
+    // slices.  The slab's odd leading dimension keeps the column-strided
+    // reads conflict-free.
     {
       const int nx = nr - rs;
       const int per = nx > 0 ? (nx + nw - 1) / nw : 0;
       const int ra = rs + wid * per, rb = min(nr, ra + per);
-      T s0 = zero_<T>(), s1 = zero_<T>();
-      Key mk = 0;
+      T s0 = zero_<T>(), s1 = zero_<T>(), g0 = zero_<T>(), g1 = zero_<T>();
+      Key mk = 0, mk2 = 0;
       if (lane >= j && lane < jb) {
         const T* pc = Ps + lane * ldp;
         int r = ra;
-        for (; r + 1 < rb; r += 2) {
-          const T x0 = col[r], x1 = col[r + 1];
-          s0 = fma_(conj_(x0), pc[r], s0);
-          s1 = fma_(conj_(x1), pc[r + 1], s1);
-          const Key k0 = mag_key(x0), k1 = mag_key(x1);
-          const Key k = k0 > k1 ? k0 : k1;
-          mk = k > mk ? k : mk;
-        }
-        if (r < rb) {
-          const T x0 = col[r];
-          s0 = fma_(conj_(x0), pc[r], s0);
-          const Key k = mag_key(x0);
-          mk = k > mk ? k : mk;
+        if (two) {
+          for (; r + 1 < rb; r += 2) {
+            const T x0 = col[r], x1 = col[r + 1];
+            const T y0 = r == jy ? zero_<T>() : col1[r];
+            const T y1 = r + 1 == jy ? zero_<T>() : col1[r + 1];
+            const T c0 = pc[r], c1 = pc[r + 1];
+            s0 = fma_(conj_(x0), c0, s0);
+            s1 = fma_(conj_(x1), c1, s1);
+            g0 = fma_(conj_(y0), c0, g0);
+            g1 = fma_(conj_(y1), c1, g1);
+            const Key k0 = mag_key(x0), k1 = mag_key(x1);
+            const Key k = k0 > k1 ? k0 : k1;
+            mk = k > mk ? k : mk;
+            const Key q0 = mag_key(y0), q1 = mag_key(y1);
+            const Key q = q0 > q1 ? q0 : q1;
+            mk2 = q > mk2 ? q : mk2;
+          }
+          if (r < rb) {
+            const T x0 = col[r];
+            const T y0 = r == jy ? zero_<T>() : col1[r];
+            const T c0 = pc[r];
+            s0 = fma_(conj_(x0), c0, s0);
+            g0 = fma_(conj_(y0), c0, g0);
+            const Key k = mag_key(x0);
+            mk = k > mk ? k : mk;
+            const Key q = mag_key(y0);
+            mk2 = q > mk2 ? q : mk2;
+          }
+        } else {
+          for (; r + 1 < rb; r += 2) {
+            const T x0 = col[r], x1 = col[r + 1];
+            s0 = fma_(conj_(x0), pc[r], s0);
+            s1 = fma_(conj_(x1), pc[r + 1], s1);
+            const Key k0 = mag_key(x0), k1 = mag_key(x1);
+            const Key k = k0 > k1 ? k0 : k1;
+            mk = k > mk ? k : mk;
+          }
+          if (r < rb) {
+            const T x0 = col[r];
+            s0 = fma_(conj_(x0), pc[r], s0);
+            const Key k = mag_key(x0);
+            mk = k > mk ? k : mk;
+          }
         }
       }
       red_w[wid][lane] = s0 + s1;
-      if (lane == j) red_k[wid] = mk;
+      if (two) red_g[wid][lane] = g0 + g1;
+      if (lane == j) {
+        red_k[wid] = mk;
+        red_k2[wid] = mk2;
+      }
     }
     if (j >= r0 && j < r0 + nr)
       for (int c = j + tid; c < jb; c += blockDim.x) {
         if constexpr (kSm) x_row[par][c] = Ps[(j - r0) + c * ldp];
         else prow[c] = Ps[(j - r0) + c * ldp];
+      }
+    if (two && jy >= 0 && jy < nr)
+      for (int c = j + tid; c < jb; c += blockDim.x) {
+        if constexpr (kSm) x_row1[par][c] = Ps[jy + c * ldp];
+        else prow1[c] = Ps[jy + c * ldp];
       }
     __syncthreads();
     if (wid == 0) {
@@ -307,15 +375,28 @@ qr_panel_kernel(PanelArgs<T> a) {
         if constexpr (kSm) x_w[par][lane] = s;
         else pw[(int64_t)b * NBMAX + lane] = s;
       }
+      if (two) {
+        T sg = zero_<T>();
+        for (int w = 0; w < nw; w++) sg += red_g[w][lane];
+        if (lane > j && lane < jb) {
+          if constexpr (kSm) x_g[par][lane] = sg;
+          else pwg[(int64_t)b * NBMAX + lane] = sg;
+        }
+      }
       if (lane == j) {
-        Key m = 0;
-        for (int w = 0; w < nw; w++) m = red_k[w] > m ? red_k[w] : m;
+        Key m = 0, m2 = 0;
+        for (int w = 0; w < nw; w++) {
+          m = red_k[w] > m ? red_k[w] : m;
+          m2 = red_k2[w] > m2 ? red_k2[w] : m2;
+        }
         if constexpr (kSm) {
           x_nrm[par][0] = re_(s);
           x_nrm[par][1] = NK::val(m);
+          x_nrm[par][2] = NK::val(m2);
         } else {
           pn[b] = re_(s);
           pn[a.gstride + b] = NK::val(m);
+          pn[2 * a.gstride + b] = NK::val(m2);
         }
       }
     }
@@ -355,57 +436,197 @@ qr_panel_kernel(PanelArgs<T> a) {
     // ---- phase B: every CTA combines the partials in the same fixed order
     // and so derives bit-identical beta / tau / w.  Warp 0: the norm; every
     // warp: a slice of the CTAs' dot partials (lane = column); lane j of
-    // warp 1 (or of warp 0 with one warp): row j.
+    // warp 1 (or of warp 0 with one warp): row j; warp 2: row j+1.
     const int NP = kH ? H : G;  // partial rows to combine
     if (wid == 0) {
       R s = R(0);
-      Key m = 0;
+      Key m = 0, m2 = 0;
       for (int q = lane; q < NP; q += 32) {
         if constexpr (kCl) {
           s += dsmem_ld(&x_nrm[par][0], (unsigned)q);
           const Key k = NK::key(dsmem_ld(&x_nrm[par][1], (unsigned)q));
           m = k > m ? k : m;
+          if (two) {
+            const Key k2 = NK::key(dsmem_ld(&x_nrm[par][2], (unsigned)q));
+            m2 = k2 > m2 ? k2 : m2;
+          }
         } else {
           s += ld_cg(&pn[q]);
           const Key k = NK::key(ld_cg(&pn[a.gstride + q]));
           m = k > m ? k : m;
+          if (two) {
+            const Key k2 = NK::key(ld_cg(&pn[2 * a.gstride + q]));
+            m2 = k2 > m2 ? k2 : m2;
+          }
         }
       }
       s = warp_sum(s);
       m = warp_max_key(m);
+      if (two) m2 = warp_max_key(m2);
       if (lane == 0) {
         sc_r[0] = s;
         sc_r[1] = NK::val(m);
         sc_flag = norm_needs_rescale<R>(m);
+        sc_flag2 = norm_needs_rescale<R>(m2);
       }
     }
     {
       const int per = (NP + nw - 1) / nw;
       const int q0 = wid * per, q1 = min(NP, q0 + per);
       T a0 = zero_<T>(), a1 = zero_<T>(), a2 = zero_<T>(), a3 = zero_<T>();
+      T b0 = zero_<T>(), b1 = zero_<T>(), b2 = zero_<T>(), b3 = zero_<T>();
       if (lane > j && lane < jb) {
         int q = q0;
         if constexpr (kCl) {
-          for (; q < q1; q++) a0 += dsmem_ld(&x_w[par][lane], (unsigned)q);
+          for (; q < q1; q++) {
+            a0 += dsmem_ld(&x_w[par][lane], (unsigned)q);
+            if (two) b0 += dsmem_ld(&x_g[par][lane], (unsigned)q);
+          }
         } else {
           for (; q + 3 < q1; q += 4) {
             a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
             a1 += ld_cg(&pw[(int64_t)(q + 1) * NBMAX + lane]);
             a2 += ld_cg(&pw[(int64_t)(q + 2) * NBMAX + lane]);
             a3 += ld_cg(&pw[(int64_t)(q + 3) * NBMAX + lane]);
+            if (two) {
+              b0 += ld_cg(&pwg[(int64_t)q * NBMAX + lane]);
+              b1 += ld_cg(&pwg[(int64_t)(q + 1) * NBMAX + lane]);
+              b2 += ld_cg(&pwg[(int64_t)(q + 2) * NBMAX + lane]);
+              b3 += ld_cg(&pwg[(int64_t)(q + 3) * NBMAX + lane]);
+            }
           }
-          for (; q < q1; q++) a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
+          for (; q < q1; q++) {
+            a0 += ld_cg(&pw[(int64_t)q * NBMAX + lane]);
+            if (two) b0 += ld_cg(&pwg[(int64_t)q * NBMAX + lane]);
+          }
         }
       }
       red_w[wid][lane] = (a0 + a1) + (a2 + a3);
+      if (two) red_g[wid][lane] = (b0 + b1) + (b2 + b3);
     }
     if (wid == (nw > 1 ? 1 : 0) && lane >= j && lane < jb) {
       // row j is held by the CTA whose rows contain j
       if constexpr (kCl) rowj[lane] = dsmem_ld(&x_row[par][lane], (unsigned)(j / rpc));
       else rowj[lane] = ld_cg(&prow[lane]);
     }
+    if (two && wid == (nw > 2 ? 2 : 0) && lane >= j && lane < jb) {
+      if constexpr (kCl) rowj1[lane] = dsmem_ld(&x_row1[par][lane], (unsigned)((j + 1) / rpc));
+      else rowj1[lane] = ld_cg(&prow1[lane]);
+    }
     __syncthreads();
     const bool rescale = sc_flag != 0;
+    if (two && !rescale) {
+      // ---- both reflectors on warp 0 (every lane derives the scalars, lane
+      // c the column-c quantities).  H_j: f_c = conj(tau) w_c as below.
+      // Column j+1 after H_j^H: with v = [1; scal x] and x_1 = A[j+1, j],
+      //   p_c = sum_{r>j+1} conj(v_r) A[r, c] = conj(scal) (d_c - conj(x_1) A[j+1, c])
+      //   q   = sum_{r>j+1} |v_r|^2 = |scal|^2 (|x|^2 - |x_1|^2)
+      //   G_c = sum_{r>j+1} conj(A'[r, j+1]) A'[r, c]
+      //       = g_c - conj(p_{j+1}) f_c - conj(f_{j+1}) p_c + conj(f_{j+1}) f_c q
+      //   A'[j+1, c] = A[j+1, c] - scal x_1 f_c,
+      // and column j+1's reflector follows from alpha = A'[j+1, j+1] and the
+      // sum of squares G_{j+1}, with d'_c = G_c (c > j+1).
+      if (wid == 0) {
+        T d = zero_<T>(), g = zero_<T>();
+        for (int w = 0; w < nw; w++) {
+          d += red_w[w][lane];
+          g += red_g[w][lane];
+        }
+        T beta, tau, scal;
+        larfg_scalars_ssq(rowj[j], sc_r[0], sc_r[1], beta, tau, scal);
+        const bool act = lane > j && lane < jb;
+        const T f = act ? conj_(tau) * fma_(conj_(scal), d, rowj[lane]) : zero_<T>();
+        const T x1 = rowj1[j];
+        const T v1 = x1 * scal;
+        const T p = act ? conj_(scal) * fma_(-conj_(x1), rowj1[lane], d) : zero_<T>();
+        const R q = abs2_(scal) * (sc_r[0] - abs2_(x1));
+        const T f1 = shfl_idx_(f, j + 1), p1 = shfl_idx_(p, j + 1);
+        const T gp = act ? (g - conj_(p1) * f - conj_(f1) * p) + (conj_(f1) * f) * q : zero_<T>();
+        const T r1 = act ? fma_(-v1, f, rowj1[lane]) : zero_<T>();
+        const R ssq1 = re_(shfl_idx_(gp, j + 1));
+        const T alpha1 = shfl_idx_(r1, j + 1);
+        const R nrm1 = re_(shfl_idx_(g, j + 1)) + abs2_(rowj1[j + 1]) + abs2_(rowj[j + 1]);
+        const bool fin = __all_sync(0xffffffffu, !act || (finite_(gp) && finite_(r1)));
+        const int en = exp2_of(nrm1);
+        const int lim = sizeof(R) == 8 ? 1000 : 100;
+        const bool ok = fin && sc_flag2 == 0 && en > -lim && en < lim && ssq1 >= R(0.5) * nrm1;
+        T beta1 = zero_<T>(), tau1 = zero_<T>(), scal1 = one_<T>(), f2 = zero_<T>();
+        if (ok) {
+          // a power of two within a factor 2 sqrt(2) of sqrt(ssq1) scales the
+          // square root in place of column j+1's largest magnitude
+          const R prox = ssq1 > R(0) ? pow2_(R(0), exp2_of(ssq1) >> 1) : R(0);
+          larfg_scalars_ssq(alpha1, ssq1, prox, beta1, tau1, scal1);
+          if (lane > j + 1 && lane < jb) f2 = conj_(tau1) * fma_(conj_(scal1), gp, r1);
+        }
+        wsh[lane] = f;
+        wsh1[lane] = f2;
+        if (lane == 0) {
+          sc[0] = beta;
+          sc[1] = tau;
+          sc[2] = scal;
+          sc1[0] = beta1;
+          sc1[1] = tau1;
+          sc1[2] = scal1;
+          sc_pair = ok ? 1 : 0;
+        }
+      }
+      __syncthreads();
+      const T beta = sc[0], tau = sc[1], scal = sc[2];
+      const bool ok = sc_pair != 0;
+      if (b == 0 && tid == 0) {
+        a.tau[j] = tau;
+        if (ok) a.tau[j + 1] = sc1[1];
+      }
+      const int rj = max(0, j - r0);
+      if (ok) {
+        // column j: scale to v; column j+1: apply H_j^H, then scale below
+        // row j+1 to v' (row j+1 becomes beta')
+        const T f1 = wsh[j + 1], scal1 = sc1[2];
+        for (int r = rj + tid; r < nr; r += blockDim.x) {
+          const int gr = r0 + r;
+          T v = one_<T>();
+          if (gr > j) {
+            v = col[r] * scal;
+            col[r] = v;
+          }
+          const T y = fma_(-v, f1, col1[r]);
+          col1[r] = gr > j + 1 ? y * scal1 : y;
+        }
+        __syncthreads();
+        // rank-2 update of the columns c > j+1: rows >= j take v f_c, rows
+        // >= j+1 also v' f'_c (v_j = 1, v'_{j+1} = 1)
+        for (int c = j + 2 + wid; c < jb; c += nw) {
+          const T fa = wsh[c], fb = wsh1[c];
+          T* pc = Ps + c * ldp;
+          for (int r = rj + lane; r < nr; r += 32) {
+            const int gr = r0 + r;
+            const T v = gr == j ? one_<T>() : col[r];
+            T y = fma_(-v, fa, pc[r]);
+            if (gr > j) y = fma_(gr == j + 1 ? -one_<T>() : -col1[r], fb, y);
+            pc[r] = y;
+          }
+        }
+        if (tid == 0 && j >= r0 && j < r0 + nr) col[j - r0] = beta;
+        if (tid == 0 && jy >= 0 && jy < nr) col1[jy] = sc1[0];
+        __syncthreads();
+        j += 2;
+      } else {
+        for (int r = rs + tid; r < nr; r += blockDim.x) col[r] = col[r] * scal;
+        __syncthreads();
+        for (int c = j + 1 + wid; c < jb; c += nw) {
+          const T f = wsh[c];
+          T* pc = Ps + c * ldp;
+          for (int r = rj + lane; r < nr; r += 32) {
+            const T v = (r0 + r == j) ? one_<T>() : col[r];
+            pc[r] = fma_(-v, f, pc[r]);
+          }
+        }
+        if (tid == 0 && j >= r0 && j < r0 + nr) col[j - r0] = beta;
+        __syncthreads();
+        j += 1;
+      }
+      continue;
+    }
     R xnorm = R(0);  // meaningful in thread 0 only (the scalars below)
     if (rescale) {
       // rare: rescale by 2^-e, e the exponent of the largest magnitude
@@ -503,6 +724,7 @@ qr_panel_kernel(PanelArgs<T> a) {
     }
     if (tid == 0 && j >= r0 && j < r0 + nr) col[j - r0] = beta;
     __syncthreads();
+    j += 1;
   }
 
   // ---- Gram partials of V (unit lower trapezoidal) for the T factor: one
@@ -941,12 +1163,13 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   T* sgn = ar.take<T>(k > 0 ? k : 1);
   T* Wpart = ar.take<T>((size_t)max_splits * nb * (wmax > 0 ? wmax : 1));
   T* W2 = ar.take<T>((size_t)nb * (wmax > 0 ? wmax : 1));
-  // norm partials [2 column parities][3][gmax] + the rescaled sums [gmax];
+  // norm partials [2 round parities][3][gmax] + the rescaled sums [gmax];
   // dot partials [2 parities][gmax][NBMAX] + the rescaled path's [gmax][NBMAX]
+  // + column j+1's [2 parities][gmax][NBMAX]
   real_t<T>* part_nrm = ar.take<real_t<T>>((size_t)7 * gmax);
-  T* part_w = ar.take<T>((size_t)3 * gmax * NBMAX);
+  T* part_w = ar.take<T>((size_t)5 * gmax * NBMAX);
   T* part_g = ar.take<T>((size_t)gmax * NBMAX * NBMAX);
-  T* alpha_buf = ar.take<T>(2 * NBMAX);  // row j of the panel, by column parity
+  T* alpha_buf = ar.take<T>(4 * NBMAX);  // rows j and j+1 of the panel, by round parity
   T* gram_buf = ar.take<T>((size_t)NBMAX * NBMAX);
   unsigned* bar = ar.take<unsigned>(2);
   int* cflag = ar.take<int>(gmax);
@@ -1036,7 +1259,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     MAK_TRY(panel_shape<T>(mp, jb, ps, s == st ? sms : lookahead_ctas()));
     PanelArgs<T> pa{A + j0 + j0 * lda, lda, (int)mp, jb, ps.rpc, tau + j0,
                     Ts + (j0 / nb) * NBMAX * NBMAX, part_nrm, part_w, part_g, alpha_buf,
-                    gram_buf, bar, cflag, status, gmax};
+                    gram_buf, bar, cflag, status, gmax, ps.sync != SYNC_HIER && tuning(TUNE_PANEL_PAIR) != 0};
     ProfScope prof(s, PROF_QR_PANEL, 2.0 * (double)mp * jb * sizeof(T));
     note_launch();
     if (ps.sync == SYNC_CLUSTER || ps.sync == SYNC_HIER) {

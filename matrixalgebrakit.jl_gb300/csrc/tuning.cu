@@ -36,6 +36,7 @@ const Param kParams[TUNE_COUNT] = {
     {"MAK_QR_OUTER64_MAX_N", 0, 0, 1073741824.0},
     {"MAK_LOOKAHEAD_CTAS", 48, 8, 120},
     {"MAK_PANEL_HIER_C", 0, 0, 8},
+    {"MAK_PANEL_PAIR", 1, 0, 1},
 };
 
 std::atomic<double> g_set[TUNE_COUNT];
