@@ -76,13 +76,26 @@ constexpr int OZ_EPI_COLS = OZ_BN * 4 / OZ_EPI_WARPS;  // output columns per epi
 constexpr int OZ_TMEM_COLS = 512;       // S group accumulators x 64 columns
 constexpr long long OZ_SPIN = 1ll << 26;
 
+// Row (column) exponents of the operands are kept as the IEEE bit patterns
+// of the largest magnitudes and decoded where they are used.
+__device__ __forceinline__ unsigned long long absbits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ int exp_of_absbits(unsigned long long b) {
+  // smallest e with |x| < 2^e (frexp exponent); 0 for x == 0
+  if (b == 0) return 0;
+  int ex = (int)(b >> 52);
+  if (ex == 0) return -1021;  // subnormal
+  return ex - 1022;
+}
+
 struct OzArgs {
   int M, Nl, nkt_total;     // logical output rows, logical output cols, K-steps in all
   int split_steps;          // K-steps per split; split z starts at K-step z * split_steps
   int tiles_m, tiles_n;     // output tiles (OZ_BM x OZ_BN) along M and N
   int splits;               // K splits; work items = tiles_m * tiles_n * splits
-  const int* EA;            // [Mpad]
-  const int* EB;            // [Nlpad]
+  const unsigned long long* bitsA;  // [Mpad] largest |A| of each row, as IEEE bits
+  const unsigned long long* bitsB;  // [Nlpad] largest |B| of each column
   double* C;                // output (FP64 view; complex: interleaved re/im)
   int64_t ldc;              // in elements of the data type
   int cpx;                  // complex output mapping
@@ -527,7 +540,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         // one rounding to FP64 by integer operations.  One loop per (alpha,
         // beta) case, so that no FP64 work of the other cases is executed
         // speculatively; C is read in batches of 8 columns.
-        const int e_row = a.EA[gi] - SH - LO_BITS;
+        const int e_row = exp_of_absbits(a.bitsA[gi]) - SH - LO_BITS;
         const double alpha = part ? 1.0 : a.alpha;
         const bool unit = alpha == 1.0 || alpha == -1.0;
         const bool flip = alpha == -1.0;
@@ -537,7 +550,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           for (int c = 0; c < OZ_EPI_COLS; c++) {
             const int gj = n0 + cb + c;
             if (gj >= a.Nl) continue;
-            const double v = fx_to_double(hi[c], (unsigned)lo[c], LO_BITS, e_row + a.EB[gj], flip);
+            const double v = fx_to_double(hi[c], (unsigned)lo[c], LO_BITS, e_row + exp_of_absbits(a.bitsB[gj]), flip);
             if (part) part[(int64_t)gj * a.M + gi] = v;  // split-K partial, ld = M
             else *oz_out_ptr(Cp, ldc, cpx, Nc, gi, gj) = v;
           }
@@ -554,7 +567,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             for (int j = 0; j < 8; j++) {
               const int c = c0 + j, gj = n0 + cb + c;
               if (gj >= a.Nl) continue;
-              double v = fx_to_double(hi[c], (unsigned)lo[c], LO_BITS, e_row + a.EB[gj], flip);
+              double v = fx_to_double(hi[c], (unsigned)lo[c], LO_BITS, e_row + exp_of_absbits(a.bitsB[gj]), flip);
               if (mode == 1) v = cv[j] + v;
               else if (mode == 2) v = fma(a.beta, cv[j], v);
               else v = fma(alpha, v, beta0 ? 0.0 : a.beta * cv[j]);
@@ -631,26 +644,21 @@ __host__ __device__ inline bool oz_contig_r(const OzSrc<T>& s) {
   return (s.side == 0) ? (s.op.op == OP_N) : (s.op.op != OP_N);
 }
 
-__device__ __forceinline__ unsigned long long absbits(double x) {
-  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-}
-__device__ __forceinline__ int exp_of_absbits(unsigned long long b) {
-  // smallest e with |x| < 2^e (frexp exponent); 0 for x == 0
-  if (b == 0) return 0;
-  int ex = (int)(b >> 52);
-  if (ex == 0) return -1021;  // subnormal
-  return ex - 1022;
-}
 
 // Row maxima of |X| as IEEE bit patterns (non-negative doubles order like
 // their bits), accumulated with atomicMax over a 2-D grid of (rows, K
 // chunks) so that tall K ranges are read by many CTAs in parallel.
 constexpr int OZ_EXP_KCHUNK = 1024;
 template <class T>
-__global__ void __launch_bounds__(256) oz_absmax_kernel(OzSrc<T> s, int R, int K,
-                                                        unsigned long long* mx_bits,
+__global__ void __launch_bounds__(256) oz_absmax_kernel(OzSrc<T> sa, int Ra,
+                                                        unsigned long long* bits_a, OzSrc<T> sb,
+                                                        int Rb, unsigned long long* bits_b, int K,
                                                         const int* skip) {
   if (skipped(skip)) return;
+  // blockIdx.z: 0 the rows of op(A), 1 the columns of op(B)
+  const OzSrc<T>& s = blockIdx.z == 0 ? sa : sb;
+  const int R = blockIdx.z == 0 ? Ra : Rb;
+  unsigned long long* mx_bits = blockIdx.z == 0 ? bits_a : bits_b;
   const int k0 = blockIdx.y * OZ_EXP_KCHUNK;
   const int k1 = min(K, k0 + OZ_EXP_KCHUNK);
   if (oz_contig_r(s)) {
@@ -681,34 +689,44 @@ __global__ void __launch_bounds__(256) oz_absmax_kernel(OzSrc<T> s, int R, int K
     if (lane == 0 && mx) atomicMax(&mx_bits[r], mx);
   }
 }
-__global__ void oz_exp_from_bits_kernel(int R, const unsigned long long* mx_bits, int* E,
-                                        const int* skip) {
-  if (skipped(skip)) return;
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < R) E[r] = exp_of_absbits(mx_bits[r]);
-}
+// Row maxima of both operands in one launch into bits_a[0, Ra) and
+// bits_b[0, Rb); the nbits words from bits_a on (which hold both) are
+// zeroed first
 template <class T>
-static int oz_exponents(cudaStream_t st, const OzSrc<T>& s, int R, int K, unsigned long long* bits,
-                        int* E) {
-  MAK_CUDA_TRY(cudaMemsetAsync(bits, 0, (size_t)R * sizeof(unsigned long long), st));
+static int oz_exponents(cudaStream_t st, const OzSrc<T>& sa, int Ra, unsigned long long* bits_a,
+                        const OzSrc<T>& sb, int Rb, unsigned long long* bits_b, int K,
+                        int64_t nbits) {
+  MAK_CUDA_TRY(cudaMemsetAsync(bits_a, 0, (size_t)nbits * sizeof(unsigned long long), st));
   const unsigned gy = (unsigned)ceil_div(K > 0 ? K : 1, OZ_EXP_KCHUNK);
-  const unsigned gx = (unsigned)(oz_contig_r(s) ? ceil_div(R, 256) : ceil_div(R, 8));
+  const int64_t gxa = oz_contig_r(sa) ? ceil_div(Ra, 256) : ceil_div(Ra, 8);
+  const int64_t gxb = oz_contig_r(sb) ? ceil_div(Rb, 256) : ceil_div(Rb, 8);
+  const unsigned gx = (unsigned)(gxa > gxb ? gxa : gxb);
   note_launch();
-  oz_absmax_kernel<T><<<dim3(gx, gy), 256, 0, st>>>(s, R, K, bits, skip_flag());
-  note_launch();
-  oz_exp_from_bits_kernel<<<(unsigned)ceil_div(R, 256), 256, 0, st>>>(R, bits, E, skip_flag());
+  oz_absmax_kernel<T><<<dim3(gx, gy, 2), 256, 0, st>>>(sa, Ra, bits_a, sb, Rb, bits_b, K,
+                                                        skip_flag());
   return cudaGetLastError() == cudaSuccess ? 0 : MAK_ERR_CUDA;
 }
 
 // planes[p][r][k] (Rpad x Kpad, bf16) = sign * digit_p * 2^(-7(p-1)), zero padded
+// (blockIdx.z: 0 the rows of op(A), 1 the columns of op(B); one launch)
+struct OzPlaneOut {
+  int R, Rpad;
+  const unsigned long long* bits;  // largest magnitude of each row, IEEE bits
+  __nv_bfloat16* planes;
+};
 template <class T, int S>
-__global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> s, int R, int K, int Rpad,
-                                                       int Kpad, const int* E,
-                                                       __nv_bfloat16* planes, const int* skip) {
+__global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> sa, OzPlaneOut oa, OzSrc<T> sb,
+                                                       OzPlaneOut ob, int K, int Kpad,
+                                                       const int* skip) {
   if (skipped(skip)) return;
+  const OzSrc<T>& s = blockIdx.z == 0 ? sa : sb;
+  const OzPlaneOut& o = blockIdx.z == 0 ? oa : ob;
+  const int R = o.R, Rpad = o.Rpad;
+  __nv_bfloat16* planes = o.planes;
+  const int r0 = blockIdx.y * 64, k0 = blockIdx.x * 64;
+  if (r0 >= Rpad) return;  // the shorter side's grid rows (uniform per CTA)
   __shared__ double tile[64][65];
   __shared__ unsigned short lut[129];  // bf16 bits of the integers -64 .. 64
-  const int r0 = blockIdx.y * 64, k0 = blockIdx.x * 64;
   const int tid = threadIdx.x;
   const bool cr = oz_contig_r(s);
   if (tid < 129) lut[tid] = __bfloat16_as_ushort(__float2bfloat16_rn((float)(tid - 64)));
@@ -731,7 +749,7 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> s, int R, int K,
     const int rr = e / 32, kp = (e % 32) * 2;
     const int r = r0 + rr;
     if (r >= Rpad) continue;
-    const int Fr = ((r < R) ? E[r] : 0) + OZ_HEADROOM;  // frame: |x| < 2^(Fr - 1)
+    const int Fr = ((r < R) ? exp_of_absbits(o.bits[r]) : 0) + OZ_HEADROOM;  // frame: |x| < 2^(Fr - 1)
     int dig[2][S];
 #pragma unroll
     for (int h = 0; h < 2; h++) {
@@ -764,6 +782,10 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> s, int R, int K,
         }
         dig[h][p] = neg ? -d : d;
       }
+      // the leading digit is at most 64 when |x| < 2^(Fr - 1); the bound
+      // also keeps the table index in range for an operand that changed
+      // between the two passes
+      cur = cur < 64 ? cur : 64;
       dig[h][0] = neg ? -cur : cur;
     }
 #pragma unroll
@@ -880,10 +902,8 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
       ceil_div(ceil_div(nkt_total, OZ_KSTEPS_PER_CHUNK), splits);
   splits = (int)ceil_div(ceil_div(nkt_total, OZ_KSTEPS_PER_CHUNK), chunks_per_split);
 
-  int* EA = ar.take<int>(Mpad);
-  int* EB = ar.take<int>(Npad);
-  unsigned long long* bitsA = ar.take<unsigned long long>(Mpad);
-  unsigned long long* bitsB = ar.take<unsigned long long>(Npad);
+  unsigned long long* bitsA = ar.take<unsigned long long>(Mpad + Npad);
+  unsigned long long* bitsB = bitsA + Mpad;
   __nv_bfloat16* PA = ar.take<__nv_bfloat16>((size_t)S * Mpad * Kpad);
   __nv_bfloat16* PB = ar.take<__nv_bfloat16>((size_t)S * Npad * Kpad);
   // split-K partials; a measuring pass reserves a bound that holds for every
@@ -906,17 +926,15 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
 
   OzSrc<T> sa{A, 0, (int)M, (int)K};
   OzSrc<T> sb{B, 1, (int)N, (int)K};
-  MAK_TRY(oz_exponents<T>(st, sa, (int)M, (int)Kl, bitsA, EA));
-  MAK_TRY(oz_exponents<T>(st, sb, (int)Nl, (int)Kl, bitsB, EB));
-  note_launch();
-  oz_split_kernel<T, S><<<dim3((unsigned)(Kpad / 64 + (Kpad % 64 ? 1 : 0)), (unsigned)(Mpad / 64)),
-                          256, 0, st>>>(sa, (int)M, (int)Kl, (int)Mpad, (int)Kpad, EA, PA,
-                                           skip_flag());
-  note_launch();
-  oz_split_kernel<T, S><<<dim3((unsigned)(Kpad / 64 + (Kpad % 64 ? 1 : 0)), (unsigned)(Npad / 64)),
-                          256, 0, st>>>(sb, (int)Nl, (int)Kl, (int)Npad, (int)Kpad, EB, PB,
-                                           skip_flag());
-  MAK_CUDA_TRY(cudaGetLastError());
+  MAK_TRY(oz_exponents<T>(st, sa, (int)M, bitsA, sb, (int)Nl, bitsB, (int)Kl, Mpad + Npad));
+  {
+    const OzPlaneOut oa{(int)M, (int)Mpad, bitsA, PA}, ob{(int)Nl, (int)Npad, bitsB, PB};
+    const int64_t rows = Mpad > Npad ? Mpad : Npad;
+    note_launch();
+    oz_split_kernel<T, S><<<dim3((unsigned)ceil_div(Kpad, 64), (unsigned)(rows / 64), 2), 256, 0,
+                            st>>>(sa, oa, sb, ob, (int)Kl, (int)Kpad, skip_flag());
+    MAK_CUDA_TRY(cudaGetLastError());
+  }
 
   CUtensorMap mapA, mapB;
   MAK_TRY(make_plane_map(&mapA, PA, S, (int)Mpad, (int)Kpad, OZ_BM));
@@ -931,7 +949,7 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
     // looping over work items
     const int split_steps = (int)(chunks_per_split * OZ_KSTEPS_PER_CHUNK);
     const int tm = (int)(Mpad / OZ_BM), tn = (int)(Npad / OZ_BN);
-    OzArgs args{(int)M, (int)Nl, (int)nkt_total, split_steps, tm, tn, splits, EA, EB,
+    OzArgs args{(int)M, (int)Nl, (int)nkt_total, split_steps, tm, tn, splits, bitsA, bitsB,
                 (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_, part, part ? M * Nl : 0,
                 status, skip_flag()};
     const int64_t nwork = (int64_t)tm * tn * splits;
