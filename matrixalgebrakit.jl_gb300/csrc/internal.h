@@ -59,6 +59,7 @@ enum TuneId {
   TUNE_LOOKAHEAD_CTAS,       // SMs of the look-ahead side stream
   TUNE_PANEL_HIER_C,         // tall panels: cooperative grid of clusters of this size (0: off)
   TUNE_PANEL_PAIR,           // QR panels: two columns per barrier round (1) or one (0)
+  TUNE_OZ_MERGED,            // split GEMM: one MMA per A plane over up to 4 B planes (1)
   TUNE_COUNT
 };
 double tuning(int id);

@@ -105,6 +105,7 @@ struct OzArgs {
   int64_t part_stride;      //   part + z * part_stride
   int* status;
   const int* skip;          // device stop flag of a fixed-iteration loop (or nullptr)
+  int merged;               // 1: one MMA per A plane and up to four B planes
 };
 
 // One work item of the persistent loop: an output tile and a K range.
@@ -145,9 +146,13 @@ __device__ __forceinline__ uint64_t oz_desc(uint32_t saddr) {
   return d;
 }
 
-// instruction descriptor: bf16 x bf16 -> fp32, K-major A and B, M=128, N=64
-constexpr uint32_t OZ_IDESC =
-    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_BN >> 3) << 17) | ((uint32_t)(OZ_BM >> 4) << 24);
+// instruction descriptor: bf16 x bf16 -> fp32, K-major A and B, M=128, N
+// columns (a multiple of 16 up to 256)
+constexpr uint32_t oz_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(OZ_BM >> 4) << 24);
+}
+constexpr uint32_t OZ_IDESC = oz_idesc(OZ_BN);
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
@@ -208,10 +213,11 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
       : "memory");
 }
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t ad, uint64_t bd, uint32_t acc) {
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t ad, uint64_t bd, uint32_t acc,
+                                     uint32_t idesc = OZ_IDESC) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(ad), "l"(bd), "r"(OZ_IDESC), "r"(acc));
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -428,17 +434,41 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           const uint32_t sb = sa + S * A_TILE;
           // group d = p + q accumulates in TMEM columns (d - 2) * 64 .. +63;
           // the first MMA of a group in a chunk overwrites its accumulator
+          if (a.merged) {
+            // A plane p against the B planes q = 1 .. S + 1 - p at once: the
+            // B plane tiles lie back to back in shared memory (one K-major
+            // operand of 64 rows per plane) and their groups p + q are
+            // adjacent TMEM column blocks, so up to four planes form one
+            // MMA of N = 256 (12 MMAs per K step instead of 36, the A tile
+            // read once per four B planes).  Plane 1's MMAs cover every
+            // group and come first.
 #pragma unroll
-          for (int d = 2; d <= S + 1; d++) {
+            for (int ks = 0; ks < OZ_BK / 16; ks++) {
 #pragma unroll
-            for (int p = 1; p < d; p++) {
-              const int q = d - p;
-#pragma unroll
-              for (int ks = 0; ks < OZ_BK / 16; ks++) {
+              for (int p = 1; p <= S; p++) {
                 const uint64_t ad = oz_desc(sa + (p - 1) * A_TILE + ks * 32);
-                const uint64_t bd = oz_desc(sb + (q - 1) * B_TILE + ks * 32);
-                umma(tmem + (d - 2) * OZ_BN, ad, bd,
-                     (chunk_first && p == 1 && ks == 0) ? 0u : 1u);
+#pragma unroll
+                for (int q0 = 1; q0 <= S + 1 - p; q0 += 4) {
+                  const int nq = (S + 2 - p - q0) < 4 ? (S + 2 - p - q0) : 4;
+                  const uint64_t bd = oz_desc(sb + (q0 - 1) * B_TILE + ks * 32);
+                  umma(tmem + (p + q0 - 2) * OZ_BN, ad, bd,
+                       (chunk_first && p == 1 && ks == 0) ? 0u : 1u, oz_idesc(nq * OZ_BN));
+                }
+              }
+            }
+          } else {
+#pragma unroll
+            for (int d = 2; d <= S + 1; d++) {
+#pragma unroll
+              for (int p = 1; p < d; p++) {
+                const int q = d - p;
+#pragma unroll
+                for (int ks = 0; ks < OZ_BK / 16; ks++) {
+                  const uint64_t ad = oz_desc(sa + (p - 1) * A_TILE + ks * 32);
+                  const uint64_t bd = oz_desc(sb + (q - 1) * B_TILE + ks * 32);
+                  umma(tmem + (d - 2) * OZ_BN, ad, bd,
+                       (chunk_first && p == 1 && ks == 0) ? 0u : 1u);
+                }
               }
             }
           }
@@ -951,7 +981,7 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
     const int tm = (int)(Mpad / OZ_BM), tn = (int)(Npad / OZ_BN);
     OzArgs args{(int)M, (int)Nl, (int)nkt_total, split_steps, tm, tn, splits, bitsA, bitsB,
                 (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_, part, part ? M * Nl : 0,
-                status, skip_flag()};
+                status, skip_flag(), tuning(TUNE_OZ_MERGED) != 0 ? 1 : 0};
     const int64_t nwork = (int64_t)tm * tn * splits;
     const int grid = (int)(nwork < cap ? nwork : cap);
     note_launch();
