@@ -397,11 +397,8 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           unsigned char* st = smem + s * STAGE;
           mbar_expect_tx(&full_bar[s], STAGE);
           const int kc = (o.kt0 + kt) * OZ_BK;
-#pragma unroll
-          for (int p = 0; p < S; p++) tma_load_3d(st + p * A_TILE, &tmA, &full_bar[s], kc, o.m0, p);
-#pragma unroll
-          for (int q = 0; q < S; q++)
-            tma_load_3d(st + S * A_TILE + q * B_TILE, &tmB, &full_bar[s], kc, o.n0, q);
+          tma_load_3d(st, &tmA, &full_bar[s], kc, o.m0, 0);
+          tma_load_3d(st + S * A_TILE, &tmB, &full_bar[s], kc, o.n0, 0);
         }
       }
       // drain: every issued stage must have landed before the CTA can exit
@@ -856,7 +853,9 @@ static int make_plane_map(CUtensorMap* map, void* base, int S, int rows_pad, int
   if (!fn) return MAK_ERR_CUDA;
   cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, (cuuint64_t)S};
   cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)rows_pad * kpad * 2};
-  cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
+  // one box holds all S planes of a K step (plane p at p * box_rows rows),
+  // so a stage takes two copies instead of 2 S
+  cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, (cuuint32_t)S};
   cuuint32_t es[3] = {1, 1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
                   CU_TENSOR_MAP_INTERLEAVE_NONE,
