@@ -60,6 +60,7 @@ enum TuneId {
   TUNE_PANEL_HIER_C,         // tall panels: cooperative grid of clusters of this size (0: off)
   TUNE_PANEL_PAIR,           // QR panels: two columns per barrier round (1) or one (0)
   TUNE_OZ_MERGED,            // split GEMM: one MMA per A plane over up to 4 B planes (1)
+  TUNE_OZ_NARROW,            // split GEMM, K <= 128: 32-wide tiles, two accumulator sets (1)
   TUNE_COUNT
 };
 double tuning(int id);

@@ -72,8 +72,7 @@ constexpr int OZ_STAGES = MAK_OZ_STAGES;  // 4 x 48 KB (K step 16): finer stages
 constexpr int OZ_EPI_WARPS = 8;         // two warps per TMEM lane quadrant
 constexpr int OZ_THREADS = 32 * (OZ_EPI_WARPS + 2);  // + TMA warp + MMA warp
 constexpr int OZ_TMA_WARP = OZ_EPI_WARPS, OZ_MMA_WARP = OZ_EPI_WARPS + 1;
-constexpr int OZ_EPI_COLS = OZ_BN * 4 / OZ_EPI_WARPS;  // output columns per epilogue thread
-constexpr int OZ_TMEM_COLS = 512;       // S group accumulators x 64 columns
+constexpr int OZ_TMEM_COLS = 512;       // S group accumulators x BN columns, per buffer
 constexpr long long OZ_SPIN = 1ll << 26;
 
 // Row (column) exponents of the operands are kept as the IEEE bit patterns
@@ -92,7 +91,7 @@ __device__ __forceinline__ int exp_of_absbits(unsigned long long b) {
 struct OzArgs {
   int M, Nl, nkt_total;     // logical output rows, logical output cols, K-steps in all
   int split_steps;          // K-steps per split; split z starts at K-step z * split_steps
-  int tiles_m, tiles_n;     // output tiles (OZ_BM x OZ_BN) along M and N
+  int tiles_m, tiles_n;     // output tiles (OZ_BM x BN) along M and N
   int splits;               // K splits; work items = tiles_m * tiles_n * splits
   const unsigned long long* bitsA;  // [Mpad] largest |A| of each row, as IEEE bits
   const unsigned long long* bitsB;  // [Nlpad] largest |B| of each column
@@ -115,12 +114,12 @@ struct OzWork {
   int m0, n0, kt0, nkt;
   double* part;
 };
-__device__ __forceinline__ OzWork oz_work(const OzArgs& a, int w) {
+__device__ __forceinline__ OzWork oz_work(const OzArgs& a, int w, int bn) {
   const int tiles = a.tiles_m * a.tiles_n;
   const int z = w / tiles, t = w - z * tiles;
   OzWork o;
   o.m0 = (t % a.tiles_m) * OZ_BM;
-  o.n0 = (t / a.tiles_m) * OZ_BN;
+  o.n0 = (t / a.tiles_m) * bn;
   o.kt0 = z * a.split_steps;
   o.nkt = min(a.nkt_total - o.kt0, a.split_steps);
   o.part = a.part ? a.part + (int64_t)z * a.part_stride : nullptr;
@@ -328,23 +327,28 @@ __device__ __forceinline__ double* oz_out_ptr(double* C, int64_t ldc, int cpx, i
 // CHUNK = K-steps per exact accumulator chunk: 32 (512 of K, group sums up
 // to 2^24, converted from their bits) or 8 (128 of K, group sums up to 2^22,
 // converted with one FFMA; products with K <= 128 use this variant).
-template <int S, int CHUNK>
+// BN = output tile width: 64, or 32 with two accumulator buffers in TMEM
+// (S x 32 columns each) so that the MMAs of the next tile run while the
+// epilogue reads the previous one.
+template <int S, int CHUNK, int BN>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
 oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                OzArgs a) {
   // a stopped iteration: every CTA leaves before any barrier or TMEM set-up
   if (skipped(a.skip)) return;
   constexpr int A_TILE = OZ_BM * OZ_ROW_BYTES;  // bytes per A-plane tile
-  constexpr int B_TILE = OZ_BN * OZ_ROW_BYTES;  // bytes per B-plane tile
+  constexpr int B_TILE = BN * OZ_ROW_BYTES;  // bytes per B-plane tile
   constexpr int STAGE = S * (A_TILE + B_TILE);
-  static_assert(S * OZ_BN <= OZ_TMEM_COLS, "one TMEM accumulator per group");
+  constexpr int NBUF = OZ_TMEM_COLS / (S * BN);  // accumulator buffers
+  constexpr int EPI_COLS = BN * 4 / OZ_EPI_WARPS;  // output columns per epilogue thread
+  static_assert(NBUF >= 1 && NBUF <= 2, "one or two TMEM accumulator sets of S groups");
   static_assert(S % 2 == 0 && S * CHUNK * OZ_BK * 64 * 64 <= (1 << 24),
                 "exact group sums over a chunk");
   constexpr bool kSmallChunk = S * CHUNK * OZ_BK * 64 * 64 <= (1 << 22);
   extern __shared__ __align__(1024) unsigned char oz_smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)oz_smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full_bar[OZ_STAGES], empty_bar[OZ_STAGES];
-  __shared__ __align__(8) uint64_t acc_full, acc_empty, drain_bar;
+  __shared__ __align__(8) uint64_t acc_full[NBUF], acc_empty[NBUF], drain_bar;
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
 
@@ -357,8 +361,10 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&acc_full, 1);
-    mbar_init(&acc_empty, 32 * OZ_EPI_WARPS);
+    for (int b = 0; b < NBUF; b++) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 32 * OZ_EPI_WARPS);
+    }
     mbar_init(&drain_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -386,7 +392,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       int it = 0;  // K-steps issued by this CTA
       bool live = true;
       for (int w = blockIdx.x; w < nwork && live; w += gridDim.x) {
-        const OzWork o = oz_work(a, w);
+        const OzWork o = oz_work(a, w, BN);
         for (int kt = 0; kt < o.nkt; kt++, it++) {
           const int s = it % OZ_STAGES;
           if (it >= OZ_STAGES &&
@@ -414,11 +420,15 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       int it = 0, ch = 0;  // K-steps consumed, accumulator chunks completed
       bool live = true;
       for (int w = blockIdx.x; w < nwork && live; w += gridDim.x) {
-        const OzWork o = oz_work(a, w);
+        const OzWork o = oz_work(a, w, BN);
         for (int kt = 0; kt < o.nkt; kt++, it++) {
           const int s = it % OZ_STAGES;
           const bool chunk_first = (kt % CHUNK) == 0;
-          if (chunk_first && ch > 0 && !mbar_wait(&acc_empty, (ch - 1) & 1, abort_flag, a.status)) {
+          // accumulator set of this chunk; its previous chunk must be drained
+          const int buf = ch % NBUF;
+          const uint32_t tacc = tmem + (uint32_t)(buf * S * BN);
+          if (chunk_first && ch >= NBUF &&
+              !mbar_wait(&acc_empty[buf], ((ch / NBUF) - 1) & 1, abort_flag, a.status)) {
             live = false;
             break;
           }
@@ -448,8 +458,8 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 for (int q0 = 1; q0 <= S + 1 - p; q0 += 4) {
                   const int nq = (S + 2 - p - q0) < 4 ? (S + 2 - p - q0) : 4;
                   const uint64_t bd = oz_desc(sb + (q0 - 1) * B_TILE + ks * 32);
-                  umma(tmem + (p + q0 - 2) * OZ_BN, ad, bd,
-                       (chunk_first && p == 1 && ks == 0) ? 0u : 1u, oz_idesc(nq * OZ_BN));
+                  umma(tacc + (p + q0 - 2) * BN, ad, bd,
+                       (chunk_first && p == 1 && ks == 0) ? 0u : 1u, oz_idesc(nq * BN));
                 }
               }
             }
@@ -463,8 +473,8 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 for (int ks = 0; ks < OZ_BK / 16; ks++) {
                   const uint64_t ad = oz_desc(sa + (p - 1) * A_TILE + ks * 32);
                   const uint64_t bd = oz_desc(sb + (q - 1) * B_TILE + ks * 32);
-                  umma(tmem + (d - 2) * OZ_BN, ad, bd,
-                       (chunk_first && p == 1 && ks == 0) ? 0u : 1u);
+                  umma(tacc + (d - 2) * BN, ad, bd,
+                       (chunk_first && p == 1 && ks == 0) ? 0u : 1u, oz_idesc(BN));
                 }
               }
             }
@@ -472,7 +482,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           umma_commit(&empty_bar[s]);
           const bool chunk_last = ((kt + 1) % CHUNK) == 0 || kt + 1 == o.nkt;
           if (chunk_last) {
-            umma_commit(&acc_full);
+            umma_commit(&acc_full[buf]);
             ch++;
           }
         }
@@ -485,17 +495,17 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     }
   } else {
     // ------------------------------------------------------------ epilogue warps 0-7
-    // thread: output row r (TMEM lane), columns cb .. cb + OZ_EPI_COLS - 1
+    // thread: output row r (TMEM lane), columns cb .. cb + EPI_COLS - 1
     constexpr int HG = S / 2;                  // groups d = 2 .. HG + 1 form the high part
     constexpr int LO_BITS = OZ_BITS * HG;      // low part: 2^-LO_BITS units of the high part
     constexpr int SH = 2 * OZ_BITS + OZ_BITS * (HG - 1) - 2 * OZ_HEADROOM;
     const int r = (warp & 3) * 32 + lane;
-    const int cb = (warp >> 2) * OZ_EPI_COLS;
+    const int cb = (warp >> 2) * EPI_COLS;
     const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)cb;
     int ch = 0;
     bool ok = true;
     for (int w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
-      const OzWork o = oz_work(a, w);
+      const OzWork o = oz_work(a, w, BN);
       const int nchunks = (o.nkt + CHUNK - 1) / CHUNK;
       double* const part = o.part;
       const bool beta0 = part != nullptr || a.beta == 0.0, beta1 = a.beta == 1.0;
@@ -503,10 +513,10 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
       double* const Cp = a.C;
       const int64_t ldc = a.ldc;
       const int cpx = a.cpx, Nc = a.Nc;
-      long long hi[OZ_EPI_COLS];  // units 2^(-OZ_BITS (HG - 1)) of the group-2 scale
-      int lo[OZ_EPI_COLS];        // units 2^(-OZ_BITS (S - 1)), in [0, 2^LO_BITS)
+      long long hi[EPI_COLS];  // units 2^(-OZ_BITS (HG - 1)) of the group-2 scale
+      int lo[EPI_COLS];        // units 2^(-OZ_BITS (S - 1)), in [0, 2^LO_BITS)
 #pragma unroll
-      for (int c = 0; c < OZ_EPI_COLS; c++) {
+      for (int c = 0; c < EPI_COLS; c++) {
         hi[c] = 0;
         lo[c] = 0;
       }
@@ -515,21 +525,22 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           // the C tile is read once, after the last chunk: pull it into L2
           // while the chunk's MMAs run
 #pragma unroll 4
-          for (int c = 0; c < OZ_EPI_COLS; c++) {
+          for (int c = 0; c < EPI_COLS; c++) {
             const int gj = n0 + cb + c;
             if (gj < a.Nl) asm volatile("prefetch.global.L2 [%0];" ::"l"(oz_out_ptr(Cp, ldc, cpx, Nc, gi, gj)));
           }
         }
-        ok = mbar_wait_backoff(&acc_full, ch & 1, abort_flag, a.status);
+        const int buf = ch % NBUF;
+        ok = mbar_wait_backoff(&acc_full[buf], (ch / NBUF) & 1, abort_flag, a.status);
         if (!ok) break;
         tc_fence_after();
         // 4 columns at a time: the register file is split over the four SM
         // sub-partitions, so with 10 warps a thread has at most 168 registers
 #pragma unroll
-        for (int c0 = 0; c0 < OZ_EPI_COLS; c0 += 4) {
+        for (int c0 = 0; c0 < EPI_COLS; c0 += 4) {
           float sv[S][4];
 #pragma unroll
-          for (int g = 0; g < S; g++) tmem_ld4(lane_addr + g * OZ_BN + c0, sv[g]);
+          for (int g = 0; g < S; g++) tmem_ld4(lane_addr + (uint32_t)((buf * S + g) * BN + c0), sv[g]);
           tmem_wait_ld();
 #pragma unroll
           for (int j = 0; j < 4; j++) {
@@ -560,7 +571,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         }
         // accumulators drained: the MMA warp may overwrite them
         tc_fence_before();
-        mbar_arrive(&acc_empty);
+        mbar_arrive(&acc_empty[buf]);
       }
       if (ok && gi < a.M) {
         // final: value = (hi 2^LO_BITS + lo) 2^(E_i + F_j - SH - LO_BITS) alpha,
@@ -574,7 +585,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         const int mode = part ? 0 : (!unit ? 3 : (beta0 ? 0 : (beta1 ? 1 : 2)));
         if (mode == 0) {
 #pragma unroll
-          for (int c = 0; c < OZ_EPI_COLS; c++) {
+          for (int c = 0; c < EPI_COLS; c++) {
             const int gj = n0 + cb + c;
             if (gj >= a.Nl) continue;
             const double v = fx_to_double(hi[c], (unsigned)lo[c], LO_BITS, e_row + exp_of_absbits(a.bitsB[gj]), flip);
@@ -583,7 +594,7 @@ oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
           }
         } else {
 #pragma unroll
-          for (int c0 = 0; c0 < OZ_EPI_COLS; c0 += 8) {
+          for (int c0 = 0; c0 < EPI_COLS; c0 += 8) {
             double cv[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
@@ -866,9 +877,9 @@ static int make_plane_map(CUtensorMap* map, void* base, int S, int rows_pad, int
   return r == CUDA_SUCCESS ? 0 : MAK_ERR_CUDA;
 }
 
-template <int S>
+template <int S, int BN>
 static size_t oz_smem_bytes() {
-  return (size_t)OZ_STAGES * S * (OZ_BM * OZ_BK * 2 + OZ_BN * OZ_BK * 2) + 1024;
+  return (size_t)OZ_STAGES * S * (OZ_BM * OZ_BK * 2 + BN * OZ_BK * 2) + 1024;
 }
 
 // the kernels' dynamic shared-memory limit, raised once per device
@@ -876,10 +887,12 @@ template <int S>
 static void oz_set_attr() {
   static PerDevice<int> pd;
   pd.get([] {
-    cudaFuncSetAttribute(oz_gemm_kernel<S, OZ_KSTEPS_PER_CHUNK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)oz_smem_bytes<S>());
-    cudaFuncSetAttribute(oz_gemm_kernel<S, OZ_SMALL_CHUNK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)oz_smem_bytes<S>());
+    cudaFuncSetAttribute(oz_gemm_kernel<S, OZ_KSTEPS_PER_CHUNK, 64>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_smem_bytes<S, 64>());
+    cudaFuncSetAttribute(oz_gemm_kernel<S, OZ_SMALL_CHUNK, 64>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_smem_bytes<S, 64>());
+    cudaFuncSetAttribute(oz_gemm_kernel<S, OZ_SMALL_CHUNK, 32>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_smem_bytes<S, 32>());
     return 1;
   });
 }
@@ -896,10 +909,16 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
   const int64_t Kl = cpx ? 2 * K : K;       // logical K
   const int64_t Nl = cpx ? 2 * N : N;       // logical output columns
   const int64_t Mpad = ceil_div(M > 0 ? M : 1, OZ_BM) * OZ_BM;
-  const int64_t Npad = ceil_div(Nl > 0 ? Nl : 1, OZ_BN) * OZ_BN;
   const int64_t Kpad = ceil_div(Kl > 0 ? Kl : 1, OZ_BK) * OZ_BK;
   const int64_t nkt_total = Kpad / OZ_BK;
-  const int64_t tiles = (Mpad / OZ_BM) * (Npad / OZ_BN);
+  // products with K <= 128 (one short chunk per tile) take 32-wide tiles with
+  // two accumulator sets, so that a tile's MMAs overlap the previous tile's
+  // epilogue; longer products the 64-wide tile (MAK_OZ_NARROW = 0: always 64)
+  const bool small = nkt_total * OZ_BK <= 128;
+  const int BN = (small && tuning(TUNE_OZ_NARROW) != 0) ? 32 : 64;
+  const int64_t Npad = ceil_div(Nl > 0 ? Nl : 1, (int64_t)BN) * BN;
+  const int64_t Npad64 = ceil_div(Nl > 0 ? Nl : 1, (int64_t)64) * 64;  // workspace bound
+  const int64_t tiles = (Mpad / OZ_BM) * (Npad / BN);
   // persistent grid cap: the caller's limit, else the thread's budget, else every SM
   if (max_ctas <= 0) max_ctas = split_gemm_cta_budget();
   const int cap = (max_ctas > 0 && max_ctas < num_sms()) ? max_ctas : num_sms();
@@ -931,10 +950,10 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
       ceil_div(ceil_div(nkt_total, OZ_KSTEPS_PER_CHUNK), splits);
   splits = (int)ceil_div(ceil_div(nkt_total, OZ_KSTEPS_PER_CHUNK), chunks_per_split);
 
-  unsigned long long* bitsA = ar.take<unsigned long long>(Mpad + Npad);
+  unsigned long long* bitsA = ar.take<unsigned long long>(Mpad + Npad64);
   unsigned long long* bitsB = bitsA + Mpad;
   __nv_bfloat16* PA = ar.take<__nv_bfloat16>((size_t)S * Mpad * Kpad);
-  __nv_bfloat16* PB = ar.take<__nv_bfloat16>((size_t)S * Npad * Kpad);
+  __nv_bfloat16* PB = ar.take<__nv_bfloat16>((size_t)S * Npad64 * Kpad);
   // split-K partials; a measuring pass reserves a bound that holds for every
   // smaller output as well (splitting happens only when tiles < SMs, and then
   // splits * tiles < 2 * SMs), because call sites measure at their largest
@@ -960,14 +979,14 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
     const OzPlaneOut oa{(int)M, (int)Mpad, bitsA, PA}, ob{(int)Nl, (int)Npad, bitsB, PB};
     const int64_t rows = Mpad > Npad ? Mpad : Npad;
     note_launch();
-    oz_split_kernel<T, S><<<dim3((unsigned)ceil_div(Kpad, 64), (unsigned)(rows / 64), 2), 256, 0,
+    oz_split_kernel<T, S><<<dim3((unsigned)ceil_div(Kpad, 64), (unsigned)ceil_div(rows, 64), 2), 256, 0,
                             st>>>(sa, oa, sb, ob, (int)Kl, (int)Kpad, skip_flag());
     MAK_CUDA_TRY(cudaGetLastError());
   }
 
   CUtensorMap mapA, mapB;
   MAK_TRY(make_plane_map(&mapA, PA, S, (int)Mpad, (int)Kpad, OZ_BM));
-  MAK_TRY(make_plane_map(&mapB, PB, S, (int)Npad, (int)Kpad, OZ_BN));
+  MAK_TRY(make_plane_map(&mapB, PB, S, (int)Npad, (int)Kpad, BN));
   oz_set_attr<S>();
 
   const double ar_ = re_(alpha), br_ = re_(beta);
@@ -977,17 +996,22 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, T alpha, Operand<T
     // persistent grid: one CTA per SM (shared memory holds one CTA), each
     // looping over work items
     const int split_steps = (int)(chunks_per_split * OZ_KSTEPS_PER_CHUNK);
-    const int tm = (int)(Mpad / OZ_BM), tn = (int)(Npad / OZ_BN);
+    const int tm = (int)(Mpad / OZ_BM), tn = (int)(Npad / BN);
     OzArgs args{(int)M, (int)Nl, (int)nkt_total, split_steps, tm, tn, splits, bitsA, bitsB,
                 (double*)C, ldc, cpx ? 1 : 0, (int)N, ar_, br_, part, part ? M * Nl : 0,
                 status, skip_flag(), tuning(TUNE_OZ_MERGED) != 0 ? 1 : 0};
     const int64_t nwork = (int64_t)tm * tn * splits;
     const int grid = (int)(nwork < cap ? nwork : cap);
     note_launch();
-    if (nkt_total * OZ_BK <= 128)  // one short chunk: the FFMA conversion
-      oz_gemm_kernel<S, OZ_SMALL_CHUNK><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
+    if (small && BN == 32)  // one short chunk: the FFMA conversion
+      oz_gemm_kernel<S, OZ_SMALL_CHUNK, 32>
+          <<<grid, OZ_THREADS, oz_smem_bytes<S, 32>(), st>>>(mapA, mapB, args);
+    else if (small)
+      oz_gemm_kernel<S, OZ_SMALL_CHUNK, 64>
+          <<<grid, OZ_THREADS, oz_smem_bytes<S, 64>(), st>>>(mapA, mapB, args);
     else
-      oz_gemm_kernel<S, OZ_KSTEPS_PER_CHUNK><<<grid, OZ_THREADS, oz_smem_bytes<S>(), st>>>(mapA, mapB, args);
+      oz_gemm_kernel<S, OZ_KSTEPS_PER_CHUNK, 64>
+          <<<grid, OZ_THREADS, oz_smem_bytes<S, 64>(), st>>>(mapA, mapB, args);
     MAK_CUDA_TRY(cudaGetLastError());
   }
   if (part) {

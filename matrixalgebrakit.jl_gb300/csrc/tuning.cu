@@ -38,6 +38,7 @@ const Param kParams[TUNE_COUNT] = {
     {"MAK_PANEL_HIER_C", 0, 0, 8},
     {"MAK_PANEL_PAIR", 1, 0, 1},
     {"MAK_OZ_MERGED", 1, 0, 1},
+    {"MAK_OZ_NARROW", 1, 0, 1},
 };
 
 std::atomic<double> g_set[TUNE_COUNT];
