@@ -682,6 +682,15 @@ __host__ __device__ inline bool oz_contig_r(const OzSrc<T>& s) {
   return (s.side == 0) ? (s.op.op == OP_N) : (s.op.op != OP_N);
 }
 
+// A real operand without a structure mask is read through its pointer
+// directly: element (r, k) of the logical operand sits at r + k ld when the
+// operand is contiguous along r, else at k + r ld (transposition is the
+// identity on real data).  Other operands go through oz_fetch.
+template <class T>
+__device__ __forceinline__ bool oz_plain(const OzSrc<T>& s) {
+  return !traits<T>::cpx && s.op.mask == MASK_FULL;
+}
+
 
 // Row maxima of |X| as IEEE bit patterns (non-negative doubles order like
 // their bits), accumulated with atomicMax over a 2-D grid of (rows, K
@@ -704,7 +713,20 @@ __global__ void __launch_bounds__(256) oz_absmax_kernel(OzSrc<T> sa, int Ra,
     const int r = blockIdx.x * 256 + threadIdx.x;
     if (r >= R) return;
     unsigned long long mx = 0;
-    for (int k = k0; k < k1; k++) {
+    int k = k0;
+    if (oz_plain(s)) {
+      // eight independent loads in flight per thread
+      const double* q = reinterpret_cast<const double*>(s.op.p) + r;
+      const int64_t ld = s.op.ld;
+      for (; k + 7 < k1; k += 8) {
+        unsigned long long b[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) b[i] = absbits(q[(int64_t)(k + i) * ld]);
+#pragma unroll
+        for (int i = 0; i < 8; i++) mx = b[i] > mx ? b[i] : mx;
+      }
+    }
+    for (; k < k1; k++) {
       const unsigned long long b = absbits(oz_fetch(s, r, k));
       mx = b > mx ? b : mx;
     }
@@ -715,7 +737,18 @@ __global__ void __launch_bounds__(256) oz_absmax_kernel(OzSrc<T> sa, int Ra,
     const int lane = threadIdx.x & 31;
     if (r >= R) return;
     unsigned long long mx = 0;
-    for (int k = k0 + lane; k < k1; k += 32) {
+    int k = k0 + lane;
+    if (oz_plain(s)) {
+      const double* q = reinterpret_cast<const double*>(s.op.p) + (int64_t)r * s.op.ld;
+      for (; k + 7 * 32 < k1; k += 8 * 32) {
+        unsigned long long b[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) b[i] = absbits(q[k + 32 * i]);
+#pragma unroll
+        for (int i = 0; i < 8; i++) mx = b[i] > mx ? b[i] : mx;
+      }
+    }
+    for (; k < k1; k += 32) {
       const unsigned long long b = absbits(oz_fetch(s, r, k));
       mx = b > mx ? b : mx;
     }
@@ -763,35 +796,61 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> sa, OzPlaneOut o
   __nv_bfloat16* planes = o.planes;
   const int r0 = blockIdx.y * 64, k0 = blockIdx.x * 64;
   if (r0 >= Rpad) return;  // the shorter side's grid rows (uniform per CTA)
-  __shared__ double tile[64][65];
+  // row stride 68 doubles: the digit phase's reads (eight rows of eight
+  // threads, eight apart in k) fall on distinct banks pairwise
+  __shared__ double tile[64][68];
   __shared__ unsigned short lut[129];  // bf16 bits of the integers -64 .. 64
   const int tid = threadIdx.x;
   const bool cr = oz_contig_r(s);
   if (tid < 129) lut[tid] = __bfloat16_as_ushort(__float2bfloat16_rn((float)(tid - 64)));
-  for (int e = tid; e < 64 * 64; e += 256) {
-    int rr, kk;
-    if (cr) { rr = e % 64; kk = e / 64; } else { kk = e % 64; rr = e / 64; }
-    const int r = r0 + rr, k = k0 + kk;
-    tile[rr][kk] = (r < R && k < K) ? oz_fetch(s, r, k) : 0.0;
+  if (oz_plain(s)) {
+    // sixteen independent loads per thread, then the stores to the tile
+    const double* src = reinterpret_cast<const double*>(s.op.p);
+    const int64_t ld = s.op.ld;
+    double v[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int e = tid + 256 * i;
+      int rr, kk;
+      if (cr) { rr = e % 64; kk = e / 64; } else { kk = e % 64; rr = e / 64; }
+      const int r = r0 + rr, k = k0 + kk;
+      v[i] = (r < R && k < K) ? src[cr ? (int64_t)r + (int64_t)k * ld : (int64_t)k + (int64_t)r * ld]
+                              : 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int e = tid + 256 * i;
+      int rr, kk;
+      if (cr) { rr = e % 64; kk = e / 64; } else { kk = e % 64; rr = e / 64; }
+      tile[rr][kk] = v[i];
+    }
+  } else {
+    for (int e = tid; e < 64 * 64; e += 256) {
+      int rr, kk;
+      if (cr) { rr = e % 64; kk = e / 64; } else { kk = e % 64; rr = e / 64; }
+      const int r = r0 + rr, k = k0 + kk;
+      tile[rr][kk] = (r < R && k < K) ? oz_fetch(s, r, k) : 0.0;
+    }
   }
   __syncthreads();
   constexpr int FB = OZ_BITS * S;  // fractional bits of the fixed-point value
   static_assert(FB <= 56, "the fixed-point value fits 28 + 28 bits");
   const size_t plane_stride = (size_t)Rpad * Kpad;
-  // each thread: one row, a pair of adjacent k.  Digits are cut with 32-bit
-  // integer operations (the value as two 28-bit halves) and each bf16 plane
-  // value d 2^(-7p) is assembled from a table of the bf16 bit patterns of the
-  // digits -64..64 by lowering the exponent field by 7p: no conversion
-  // instructions.
-  for (int e = tid; e < 64 * 32; e += 256) {
-    const int rr = e / 32, kp = (e % 32) * 2;
+  // each thread: one row, eight adjacent k (one 16-byte store per plane).
+  // Digits are cut with 32-bit integer operations (the value as two 28-bit
+  // halves) and each bf16 plane value d 2^(-7p) is assembled from a table of
+  // the bf16 bit patterns of the digits -64..64 by lowering the exponent
+  // field by 7p: no conversion instructions.
+  for (int e = tid; e < 64 * 8; e += 256) {
+    const int rr = e / 8, kq = (e % 8) * 8;
     const int r = r0 + rr;
-    if (r >= Rpad) continue;
+    const int k = k0 + kq;
+    if (r >= Rpad || k >= Kpad) continue;
     const int Fr = ((r < R) ? exp_of_absbits(o.bits[r]) : 0) + OZ_HEADROOM;  // frame: |x| < 2^(Fr - 1)
-    int dig[2][S];
+    unsigned packed[S][4];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const double x = tile[rr][kp + h];
+    for (int h = 0; h < 8; h++) {
+      const double x = tile[rr][kq + h];
       const unsigned long long bts = (unsigned long long)__double_as_longlong(x);
       const bool neg = (bts >> 63) != 0;
       int ex = (int)((bts >> 52) & 0x7FF);
@@ -809,6 +868,7 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> sa, OzPlaneOut o
       // lowest digits, the carry then continues into the high half
       const int hi28 = (int)(f >> 28);
       int cur = (int)(f & 0xFFFFFFFull);
+      int dig[S];
 #pragma unroll
       for (int p = S - 1; p >= 1; p--) {
         if (p == S - 5) cur += hi28;
@@ -818,24 +878,25 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> sa, OzPlaneOut o
           d -= 128;
           cur += 1;
         }
-        dig[h][p] = neg ? -d : d;
+        dig[p] = neg ? -d : d;
       }
       // the leading digit is at most 64 when |x| < 2^(Fr - 1); the bound
       // also keeps the table index in range for an operand that changed
       // between the two passes
       cur = cur < 64 ? cur : 64;
-      dig[h][0] = neg ? -cur : cur;
+      dig[0] = neg ? -cur : cur;
+#pragma unroll
+      for (int p = 0; p < S; p++) {
+        unsigned b = lut[dig[p] + 64];
+        b = (b & 0x7FFFu) ? b - (unsigned)(OZ_BITS * p << 7) : b;
+        if (h & 1) packed[p][h >> 1] |= b << 16;
+        else packed[p][h >> 1] = b;
+      }
     }
 #pragma unroll
-    for (int p = 0; p < S; p++) {
-      unsigned b0 = lut[dig[0][p] + 64], b1 = lut[dig[1][p] + 64];
-      b0 = (b0 & 0x7FFFu) ? b0 - (unsigned)(OZ_BITS * p << 7) : b0;
-      b1 = (b1 & 0x7FFFu) ? b1 - (unsigned)(OZ_BITS * p << 7) : b1;
-      const int k = k0 + kp;
-      if (k < Kpad)
-        *reinterpret_cast<unsigned*>(planes + p * plane_stride + (size_t)r * Kpad + k) =
-            b0 | (b1 << 16);
-    }
+    for (int p = 0; p < S; p++)
+      *reinterpret_cast<uint4*>(planes + p * plane_stride + (size_t)r * Kpad + k) =
+          make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
   }
 }
 
