@@ -22,6 +22,7 @@ from .algorithms import (ArgumentError, DimensionMismatch, GB300_HouseholderQR,
                          GB300_PolarNewton, LeftOrthViaPolar, LeftOrthViaQR, LQViaTransposedQR,
                          default_algorithm, is_positive, select_algorithm)
 from .blas import gemm
+from .core import check_info, new_info
 from .lq import lq_compact, lq_compact_, lq_full, lq_full_, lq_null, lq_null_
 from .polar import SingularException, left_polar, left_polar_, right_polar, right_polar_
 from .qr import (initialize_output, qr_compact, qr_compact_, qr_full, qr_full_, qr_null,
@@ -33,7 +34,7 @@ __all__ = [
     "select_algorithm", "is_positive", "qr_compact", "qr_compact_", "qr_full", "qr_full_",
     "qr_null", "qr_null_", "left_polar", "left_polar_", "initialize_output", "library", "gemm",
     "LQViaTransposedQR", "lq_compact", "lq_compact_", "lq_full", "lq_full_", "lq_null",
-    "lq_null_", "right_polar", "right_polar_",
+    "lq_null_", "right_polar", "right_polar_", "new_info", "check_info",
 ]
 
 

@@ -89,6 +89,7 @@ def workspace(nbytes: int, device):
 
 
 def new_info(device):
+    """A device outcome record (``mak_info``) for a call to write."""
     return torch.zeros(INFO_BYTES, dtype=torch.uint8, device=device)
 
 
@@ -113,6 +114,12 @@ def check_rc(rc: int, fname: str, argnames=()):
     if rc == _lib.MAK_ERR_UNSUPPORTED:
         raise ArgumentError(f"{fname}: {msg}")
     raise RuntimeError(f"{fname}: {msg} (code {rc})")
+
+
+def check_info(info_t, fname: str = "mak_gb300"):
+    """Read a device outcome record (synchronizes its stream) and raise if
+    the call that wrote it failed on the device."""
+    check_status(read_info(info_t), fname)
 
 
 def check_status(info: _lib.mak_info, fname: str):

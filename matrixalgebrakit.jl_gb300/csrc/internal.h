@@ -61,6 +61,8 @@ enum TuneId {
   TUNE_PANEL_PAIR,           // QR panels: two columns per barrier round (1) or one (0)
   TUNE_OZ_MERGED,            // split GEMM: one MMA per A plane over up to 4 B planes (1)
   TUNE_OZ_NARROW,            // split GEMM, K <= 128: 32-wide tiles, two accumulator sets (1)
+  TUNE_LOOKAHEAD_TAIL_COLS,  // far columns from which down the side stream gets more SMs
+  TUNE_LOOKAHEAD_TAIL_CTAS,  // the side stream's SMs in that tail
   TUNE_COUNT
 };
 double tuning(int id);

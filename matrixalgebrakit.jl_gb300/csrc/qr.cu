@@ -847,6 +847,14 @@ constexpr int QR_OUTER_NB = 128;  // outer block of the mixed-precision path
 // the main stream's persistent tensor-core grid takes the rest; 48 by
 // default, MAK_LOOKAHEAD_CTAS overrides it (read once, clamped to 8..120).
 int lookahead_ctas() { return (int)tuning(TUNE_LOOKAHEAD_CTAS); }
+// In the tail of the factorization the far update shrinks below the time
+// of the next block's panels; from MAK_LOOKAHEAD_TAIL_COLS far columns
+// down, the side stream takes MAK_LOOKAHEAD_TAIL_CTAS SMs instead.
+static int side_ctas(int64_t far_cols) {
+  const double tail = tuning(TUNE_LOOKAHEAD_TAIL_COLS);
+  return (double)far_cols <= tail ? (int)tuning(TUNE_LOOKAHEAD_TAIL_CTAS) : lookahead_ctas();
+}
+static thread_local int tl_side_ctas = 0;  // the side stream's SMs for the block being factored
 
 static thread_local bool tl_no_lookahead = false;
 bool lookahead_enabled() { return !tl_no_lookahead; }
@@ -1256,7 +1264,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
   auto panel = [&](int64_t j0, int jb, cudaStream_t s) -> int {
     const int64_t mp = m - j0;
     PanelShape ps;
-    MAK_TRY(panel_shape<T>(mp, jb, ps, s == st ? sms : lookahead_ctas()));
+    MAK_TRY(panel_shape<T>(mp, jb, ps, s == st ? sms : tl_side_ctas));
     PanelArgs<T> pa{A + j0 + j0 * lda, lda, (int)mp, jb, ps.rpc, tau + j0,
                     Ts + (j0 / nb) * NBMAX * NBMAX, part_nrm, part_w, part_g, alpha_buf,
                     gram_buf, bar, cflag, status, gmax, ps.sync != SYNC_HIER && tuning(TUNE_PANEL_PAIR) != 0};
@@ -1308,7 +1316,7 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
       MAK_TRY(gemm_prec<T>(s, precision, JB, JB, m - J0, one_<T>(),
                            opnd<T>(V, lda, OP_C, MASK_UNIT_LOWER),
                            opnd<T>(V, lda, OP_N, MASK_UNIT_LOWER), zero_<T>(), Gm, NBO, ga,
-                           status, s == st ? 0 : lookahead_ctas()));
+                           status, s == st ? 0 : tl_side_ctas));
     }
     note_launch();
     larft_cols_kernel<T><<<(unsigned)ceil_div(JB, 8), 256, 0, s>>>(JB, Gm, NBO, tau + J0,
@@ -1344,10 +1352,12 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
       MAK_TRY(apply_block(b, nx, nx_end, st, 0));
       MAK_CUDA_TRY(cudaEventRecord(la->ev_ready, st));
       MAK_CUDA_TRY(cudaStreamWaitEvent(la->side, la->ev_ready, 0));
+      tl_side_ctas = side_ctas(n - nx_end);
+      if (tl_side_ctas > sms - 8) tl_side_ctas = sms - 8;
       MAK_TRY(factor_block(b + 1, la->side));
       MAK_CUDA_TRY(cudaEventRecord(la->ev_done, la->side));
       // the persistent tensor-core grid leaves the side stream its SMs
-      MAK_TRY(apply_block(b, nx_end, n, st, sms - lookahead_ctas()));
+      MAK_TRY(apply_block(b, nx_end, n, st, sms - tl_side_ctas));
       MAK_CUDA_TRY(cudaStreamWaitEvent(st, la->ev_done, 0));
     } else {
       MAK_TRY(apply_block(b, nx, n, st, 0));

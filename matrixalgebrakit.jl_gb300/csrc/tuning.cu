@@ -39,6 +39,8 @@ const Param kParams[TUNE_COUNT] = {
     {"MAK_PANEL_PAIR", 1, 0, 1},
     {"MAK_OZ_MERGED", 1, 0, 1},
     {"MAK_OZ_NARROW", 1, 0, 1},
+    {"MAK_LOOKAHEAD_TAIL_COLS", 4096, 0, 1073741824.0},
+    {"MAK_LOOKAHEAD_TAIL_CTAS", 96, 8, 144},
 };
 
 std::atomic<double> g_set[TUNE_COUNT];

@@ -82,20 +82,27 @@ def _qr_bang(A, QR, alg, full: bool, info_out=None):
     return Q, R
 
 
-def qr_compact_(A, QR=None, alg=None, **kwargs):
-    """``qr_compact!(A, (Q, R), alg)``: destroys A, returns the passed Q, R."""
+def qr_compact_(A, QR=None, alg=None, info=None, **kwargs):
+    """``qr_compact!(A, (Q, R), alg)``: destroys A, returns the passed Q, R.
+
+    Like the reference, the call checks the device's outcome record before
+    it returns (one host synchronization).  With ``info`` (a record from
+    ``new_info(device)``) it returns as soon as the work is queued on the
+    current stream, as the C ABI does, and the caller checks the record
+    later with ``check_info`` (so that copies and the next calls overlap)."""
     alg = select_algorithm("qr_compact_", A, alg, **kwargs)
     if QR is None:
         QR = initialize_output("qr_compact_", A)
-    return _qr_bang(A, QR, alg, full=False)
+    return _qr_bang(A, QR, alg, full=False, info_out=info)
 
 
-def qr_full_(A, QR=None, alg=None, **kwargs):
-    """``qr_full!(A, (Q, R), alg)``: Q is m x m, R is m x n."""
+def qr_full_(A, QR=None, alg=None, info=None, **kwargs):
+    """``qr_full!(A, (Q, R), alg)``: Q is m x m, R is m x n (``info`` as for
+    ``qr_compact_``)."""
     alg = select_algorithm("qr_full_", A, alg, **kwargs)
     if QR is None:
         QR = initialize_output("qr_full_", A)
-    return _qr_bang(A, QR, alg, full=True)
+    return _qr_bang(A, QR, alg, full=True, info_out=info)
 
 
 def qr_compact(A, alg=None, **kwargs):

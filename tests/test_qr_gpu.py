@@ -91,6 +91,25 @@ def test_qr_bang_returns_same_objects_and_empty_r(mak, cuda):
     assert O.rel_err(to_host(Q3), O.qr_compact(A)[0]) <= 1e-12
 
 
+def test_qr_bang_deferred_info(mak, cuda):
+    """info=: the calls return once queued; a stream of factorizations into
+    the same outputs matches the oracle, and the records read back clean."""
+    rng = np.random.default_rng(3)
+    As = [O.gaussian(rng, 300, 200, np.float64) for _ in range(3)]
+    infos = [mak.new_info(cuda) for _ in As]
+    Q, R = mak.initialize_output("qr_compact_", to_dev(As[0], cuda))
+    Rs = []
+    for A, inf in zip(As, infos):
+        mak.qr_compact_(to_dev(A, cuda), (Q, R), info=inf, precision="mixed")
+        Rs.append(R.clone())
+    for A, Rd, inf in zip(As, Rs, infos):
+        mak.check_info(inf, "qr_compact_")
+        assert O.rel_err(to_host(Rd), O.qr_compact(A)[1]) <= 1e-12
+    Qf, Rf = mak.qr_full_(to_dev(As[0], cuda), info=infos[0])
+    mak.check_info(infos[0])
+    assert O.qr_residual(As[0], to_host(Qf), to_host(Rf)) <= 1e-13
+
+
 def test_qr_positive_false_and_blocksizes(mak, cuda):
     rng = np.random.default_rng(2)
     A = O.gaussian(rng, 70, 45, np.complex128)
