@@ -148,9 +148,11 @@ class ClockSampler:
     def __init__(self, uuid: str):
         self.uuid = uuid.replace("GPU-", "")
         self.proc = None
-        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.tmp = None
 
     def start(self):
+        """Start sampling (again: every start/stop pair is its own record)."""
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
@@ -579,11 +581,13 @@ def run_gb300(args):
     # the next step without waiting; every record is checked after the
     # timed region.
     if not args.no_e2e and not args.lean:
-        A0_, Q0_, R0_, alg = r["A"], r["Q"], r["R"], r["alg"]
+        alg = r["alg"]
+        A0_ = r["A"]
+        Q0_, R0_ = mak.initialize_output("qr_compact_", A0_)
         A_pin = torch.empty((n, m), dtype=torch.float64).pin_memory().t()
         A_pin.copy_(A_host)
-        bufs = [(A0_, Q0_, R0_), (torch.empty_like(A0_), torch.empty_like(Q0_),
-                                  torch.empty_like(R0_))]
+        bufs = [(torch.empty_like(A0_),) + tuple(mak.initialize_output("qr_compact_", A0_))
+                for _ in range(2)]
         pins = [(torch.empty((Q0_.shape[1], Q0_.shape[0]), dtype=torch.float64).pin_memory().t(),
                  torch.empty((R0_.shape[1], R0_.shape[0]), dtype=torch.float64).pin_memory().t())
                 for _ in range(2)]
@@ -623,6 +627,7 @@ def run_gb300(args):
         if dist is not None:
             dist.barrier()
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clocks.start()
         s0.record(s_comp)
         s_h2d.wait_stream(s_comp)
         s_d2h.wait_stream(s_comp)
@@ -632,6 +637,7 @@ def run_gb300(args):
         s_comp.wait_stream(s_d2h)
         s1.record(s_comp)
         torch.cuda.synchronize()
+        e2e_clk = clocks.stop()
         if dist is not None:
             dist.barrier()
         for inf in infos:
@@ -643,7 +649,8 @@ def run_gb300(args):
                       "d2h_bytes_per_step": int((Q0_.numel() + R0_.numel()) * 8),
                       "overlap": "double-buffered: step i's copies overlap the kernels of "
                                  "step i+1 (H2D and D2H streams, event-ordered); each call's "
-                                 "device outcome record checked after the timed region"}
+                                 "device outcome record checked after the timed region",
+                      "clocks": e2e_clk}
         del A_pin, pins, bufs
     del r
 

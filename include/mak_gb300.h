@@ -135,6 +135,15 @@ int mak_profile_read(int kind, double* total_ms, double* total_work, uint64_t* l
  *                          of that many CTAs combine through distributed
  *                          shared memory and only their leaders meet at the
  *                          grid barrier (0)
+ *   MAK_PANEL_PAIR         QR panels: two columns per barrier round where the
+ *                          norms allow (1), or one (0)
+ *   MAK_OZ_MERGED          split GEMM: one MMA per A plane over up to four B
+ *                          planes (1), or one MMA per plane pair (0)
+ *   MAK_OZ_NARROW          split GEMM with K <= 128: 32-wide tiles with two
+ *                          accumulator sets (1), or 64-wide tiles (0)
+ *   MAK_LOOKAHEAD_TAIL_COLS / MAK_LOOKAHEAD_TAIL_CTAS  from this many far
+ *                          columns down, the look-ahead side stream takes
+ *                          this many SMs (4096, 96)
  * mak_tuning_set: 0 ok, -1 unknown name, -2 value out of range; a NaN value
  * returns the parameter to its environment / default value.
  * mak_tuning_get: the value in effect.  mak_tuning_name(i): the i-th name,
