@@ -55,10 +55,11 @@ OZ_PAIRS = 36  # bf16 plane products per FP64 product in the split GEMM (8 slice
 # K = 8192; summary in profiles/oz_gemm_kernel_trailing_update_shapes.md).
 # Both grow in proportion to the work, so the per-launch traffic is this
 # rate times the launch's FP64-equivalent flops.
-OZ_TRAFFIC = {"bytes_per_fp64_flop": 0.0626,
+OZ_TRAFFIC = {"bytes_per_fp64_flop": 0.0635,
               "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of oz_gemm_kernel on "
-                        "8192x4096x128 and 128x4096x8192 (bench.py --workload gemm), scaled by "
-                        "the launch's FP64-equivalent flops"}
+                        "16384x8192x128 (2.173 GB) and 128x8192x16384 (2.194 GB), 34.4 GFLOP "
+                        "FP64-equivalent each (bench.py --workload gemm), scaled by the "
+                        "launch's FP64-equivalent flops"}
 
 
 def parse():
