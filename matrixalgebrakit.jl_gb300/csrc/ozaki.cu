@@ -799,10 +799,16 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> sa, OzPlaneOut o
   // row stride 68 doubles: the digit phase's reads (eight rows of eight
   // threads, eight apart in k) fall on distinct banks pairwise
   __shared__ double tile[64][68];
-  __shared__ unsigned short lut[129];  // bf16 bits of the integers -64 .. 64
+  // bf16 bits of +-(t - 64) 2^(-7p) for the biased digits t = 0 .. 128 of
+  // plane p ([0]: positive values, [1]: negated)
+  __shared__ unsigned short lut[2][S][130];
   const int tid = threadIdx.x;
   const bool cr = oz_contig_r(s);
-  if (tid < 129) lut[tid] = __bfloat16_as_ushort(__float2bfloat16_rn((float)(tid - 64)));
+  for (int e = tid; e < 2 * S * 129; e += 256) {
+    const int sg = e / (S * 129), p = (e / 129) % S, t = e % 129;
+    const float v = ldexpf((float)(t - 64), -OZ_BITS * p);
+    lut[sg][p][t] = __bfloat16_as_ushort(__float2bfloat16_rn(sg && t != 64 ? -v : v));
+  }
   if (oz_plain(s)) {
     // sixteen independent loads per thread, then the stores to the tile
     const double* src = reinterpret_cast<const double*>(s.op.p);
@@ -863,32 +869,26 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzSrc<T> sa, OzPlaneOut o
       else if (sh >= 0) f = (sh >= 11) ? 0 : (m << sh);
       else if (-sh >= 55) f = 0;
       else f = (m >> (-sh)) + ((m >> (-sh - 1)) & 1ull);
-      // balanced base-2^7 digits from the bottom: d_p in [-64, 63] for
-      // p >= 1, leading digit in [0, 64]; the low 28-bit half holds the four
-      // lowest digits, the carry then continues into the high half
-      const int hi28 = (int)(f >> 28);
-      int cur = (int)(f & 0xFFFFFFFull);
-      int dig[S];
-#pragma unroll
-      for (int p = S - 1; p >= 1; p--) {
-        if (p == S - 5) cur += hi28;
-        int d = cur & 127;
-        cur >>= OZ_BITS;
-        if (d >= 64) {
-          d -= 128;
-          cur += 1;
-        }
-        dig[p] = neg ? -d : d;
-      }
-      // the leading digit is at most 64 when |x| < 2^(Fr - 1); the bound
-      // also keeps the table index in range for an operand that changed
-      // between the two passes
-      cur = cur < 64 ? cur : 64;
-      dig[0] = neg ? -cur : cur;
+      // balanced base-2^7 digits d_p (plane p weighs 2^(-7p)): d_p in
+      // [-64, 63] below the leading digit, which is in [0, 64].  Adding
+      // 64 to every digit position (the constant BIAS) turns the balanced
+      // digits into the plain base-128 digits t_p = d_p + 64 of f + BIAS, so
+      // each is one shift and one mask, with no carries
+      constexpr unsigned long long BIAS = [] {
+        unsigned long long b = 0;
+        for (int i = 0; i < S; i++) b |= 64ull << (OZ_BITS * i);
+        return b;
+      }();
+      const unsigned long long u = f + BIAS;
+      const unsigned short* tb = &lut[neg ? 1 : 0][0][0];
 #pragma unroll
       for (int p = 0; p < S; p++) {
-        unsigned b = lut[dig[p] + 64];
-        b = (b & 0x7FFFu) ? b - (unsigned)(OZ_BITS * p << 7) : b;
+        unsigned t = (unsigned)(u >> (OZ_BITS * (S - 1 - p)));
+        // the leading digit is at most 64 when |x| < 2^(Fr - 1); the bound
+        // also keeps the table index in range for an operand that changed
+        // between the two passes
+        t = p == 0 ? (t < 128u ? t : 128u) : (t & 127u);
+        const unsigned b = tb[p * 130 + t];
         if (h & 1) packed[p][h >> 1] |= b << 16;
         else packed[p][h >> 1] = b;
       }
