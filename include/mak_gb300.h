@@ -144,6 +144,9 @@ int mak_profile_read(int kind, double* total_ms, double* total_work, uint64_t* l
  *   MAK_LOOKAHEAD_TAIL_COLS / MAK_LOOKAHEAD_TAIL_CTAS  from this many far
  *                          columns down, the look-ahead side stream takes
  *                          this many SMs (4096, 96)
+ *   MAK_SMALL_QR_BYTES     batched QR: blocks of at most this many bytes (m n
+ *                          + 2 min(m,n) elements) are factored by the one-CTA
+ *                          small-block kernel (0 = off; 200704)
  * mak_tuning_set: 0 ok, -1 unknown name, -2 value out of range; a NaN value
  * returns the parameter to its environment / default value.
  * mak_tuning_get: the value in effect.  mak_tuning_name(i): the i-th name,
@@ -362,6 +365,23 @@ int mak_batched_qr_compact(const mak_batch_item* items, int nitems, const mak_qr
                            void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream);
 int mak_batched_left_polar_workspace(const mak_batch_item* items, int nitems,
                                      const mak_polar_opts* opts, size_t* bytes);
+/* Small blocks (no counterpart in the reference: qr_compact! per block,
+ * src/implementations/qr.jl:132-188).  A QR block whose m x n elements (plus
+ * 2 min(m,n)) fit mak_small_qr_max_bytes() bytes is factored by ONE CTA in
+ * shared memory; mak_batched_qr_compact sends all such blocks of a call to
+ * one persistent launch (its items copied into the launch's parameters)
+ * beside the internal streams that take the larger ones.
+ * mak_batched_qr_compact_device takes the work list in DEVICE memory
+ * (`items`: nitems mak_batch_item records, e.g. written by a previous
+ * kernel; read by the kernel, so the host never sees the shapes): every item
+ * is factored by the one-CTA kernel (opts->positive honoured), and an item
+ * that does not fit reports MAK_ERR_UNSUPPORTED in its record.  No
+ * workspace; `infos` is a DEVICE array of nitems records.
+ * mak_small_qr_max_bytes: the shared memory a block may take (the tuning
+ * value MAK_SMALL_QR_BYTES, default 196 KiB, capped by the device; 0 = off). */
+int mak_batched_qr_compact_device(const mak_batch_item* items, int nitems,
+                                  const mak_qr_opts* opts, mak_info* infos, mak_stream_t stream);
+int mak_small_qr_max_bytes(void);
 int mak_batched_left_polar(const mak_batch_item* items, int nitems, const mak_polar_opts* opts,
                            void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream);
 

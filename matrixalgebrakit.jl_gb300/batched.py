@@ -84,6 +84,62 @@ def batched_qr_compact(As, alg=None, copy_inputs=True, outs=None, _capturing=Fal
     return outs
 
 
+def small_qr_max_bytes() -> int:
+    """Shared memory (bytes) a block may take in the one-CTA small-block QR:
+    m n + 2 min(m, n) elements (0: the kernel is switched off)."""
+    return int(lib().mak_small_qr_max_bytes())
+
+
+def batch_items_device(As, outs):
+    """The work list of ``As`` / ``outs`` as a DEVICE array of
+    ``mak_batch_item`` records (a uint8 tensor), the layout a caller's own
+    kernel may also write."""
+    items = _items(As, outs)
+    raw = torch.frombuffer(bytearray(bytes(items)), dtype=torch.uint8)
+    return raw.to(As[0].device)
+
+
+def batched_qr_compact_device(As, alg=None, copy_inputs=True, outs=None, items=None,
+                              _capturing=False, **kwargs):
+    """qr_compact of every block from a work list in DEVICE memory
+    (``mak_batched_qr_compact_device``): one persistent launch in which each
+    CTA factors whole blocks in shared memory; every block must fit
+    ``small_qr_max_bytes()``.  ``items`` (from ``batch_items_device``) may be
+    passed to reuse a list; returns [(Q_i, R_i)]."""
+    alg = select_algorithm("qr_compact_", None, alg, **kwargs)
+    if not As:
+        return []
+    dev = As[0].device
+    for A in As:
+        check_cuda_tensor(A, "A")
+        if A.device != dev:
+            raise ArgumentError("all blocks must live on one device")
+    if outs is None:
+        outs = []
+        for A in As:
+            m, n = A.shape
+            k = min(m, n)
+            outs.append((empty_cm(m, k, A.dtype, A.device), empty_cm(k, n, A.dtype, A.device)))
+    work_As = [to_cm(A) for A in As] if copy_inputs else list(As)
+    if items is None:
+        items = batch_items_device(work_As, outs)
+    opts = _lib.mak_qr_opts(int(alg.positive), int(alg.blocksize), PRECISION_CODE[alg.precision], 0)
+    L = lib()
+    with torch.cuda.device(dev):
+        infos = torch.zeros(len(As) * INFO_BYTES, dtype=torch.uint8, device=dev)
+        rc = L.mak_batched_qr_compact_device(items.data_ptr(), len(As), ct.byref(opts),
+                                             infos.data_ptr(), stream_handle(dev))
+        check_rc(rc, "mak_batched_qr_compact_device")
+        if _capturing:
+            return outs
+        res = _read_infos(infos, len(As))
+    for i, inf in enumerate(res):
+        if inf.status != 0:
+            raise RuntimeError(f"mak_batched_qr_compact_device: block {i}: device status "
+                               f"{inf.status}")
+    return outs
+
+
 def batched_left_polar(As, alg=None, copy_inputs=True, outs=None, _capturing=False, _info=None,
                        **kwargs):
     """left_polar of every block; returns [(W_i, P_i)].  Without host

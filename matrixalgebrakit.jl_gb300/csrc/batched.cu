@@ -101,7 +101,8 @@ static double item_flops(int kind, const mak_batch_item& it) {
 }
 
 struct Plan {
-  std::vector<int> owner;            // stream of each item
+  std::vector<int> owner;            // stream of each item (-1: the one-CTA small-block launch)
+  std::vector<int> small;            // items factored by the one-CTA small-block kernel
   std::vector<size_t> ws_item;       // workspace of each item
   size_t ws_stream[kMaxBatchStreams];   // slice size per stream
   size_t off[kMaxBatchStreams];
@@ -112,9 +113,18 @@ struct Plan {
 static int plan(int kind, const mak_batch_item* items, int nitems, const void* opts, Plan& p) {
   p.owner.assign(nitems, 0);
   p.ws_item.assign(nitems, 0);
-  std::vector<int> order(nitems);
+  p.small.clear();
+  // QR blocks that fit one CTA's shared memory go to one persistent launch
+  const int small_cap = kind == BATCH_QR ? small_qr_cap() : 0;
+  std::vector<int> order;
+  order.reserve(nitems);
   for (int i = 0; i < nitems; i++) {
-    order[i] = i;
+    if (small_qr_fits(items[i], small_cap)) {
+      p.owner[i] = -1;
+      p.small.push_back(i);
+      continue;
+    }
+    order.push_back(i);
     Arena meas(nullptr, 0);
     mak_batch_item probe = items[i];
     probe.A = probe.Q = probe.R = nullptr;
@@ -177,6 +187,13 @@ static int batched(int kind, const mak_batch_item* items, int nitems, const void
     return item_flops(kind, items[a]) > item_flops(kind, items[b]);
   });
   int rc_all = 0;
+  if (!p.small.empty()) {
+    // the small blocks: one persistent launch on the caller's stream, which
+    // runs beside the internal streams (forked above, joined below)
+    const mak_qr_opts* o = (const mak_qr_opts*)opts;
+    rc_all = small_qr_launch(st, items, p.small.data(), (int)p.small.size(), o->positive, infos,
+                             small_qr_cap());
+  }
   {
     // the batch's streams already overlap the blocks (no look-ahead), and a
     // quarter of the SMs per split product lets several blocks' persistent
@@ -184,6 +201,7 @@ static int batched(int kind, const mak_batch_item* items, int nitems, const void
     ThreadSettingsScope settings(false, (int)tuning(TUNE_BATCH_GEMM_CTAS));
     for (int i : order) {
       const int s = p.owner[i];
+      if (s < 0) continue;  // in the small-block launch
       Arena ar((char*)work + p.off[s], p.ws_stream[s]);
       int rc = info_reset(sp.s[s], infos + i);
       if (rc == 0) rc = item_dispatch(kind, items[i], opts, ar, infos + i, sp.s[s]);

@@ -63,9 +63,19 @@ enum TuneId {
   TUNE_OZ_NARROW,            // split GEMM, K <= 128: 32-wide tiles, two accumulator sets (1)
   TUNE_LOOKAHEAD_TAIL_COLS,  // far columns from which down the side stream gets more SMs
   TUNE_LOOKAHEAD_TAIL_CTAS,  // the side stream's SMs in that tail
+  TUNE_SMALL_QR_BYTES,       // batched QR: blocks up to this many bytes take the one-CTA kernel
   TUNE_COUNT
 };
 double tuning(int id);
+
+// one-CTA Householder QR of small blocks from a work list (small.cu): the
+// shared memory a CTA gives its block (0: off), whether an item fits, and
+// one persistent launch over the listed items (`which` indexes `items` and
+// `infos`)
+int small_qr_cap();
+bool small_qr_fits(const mak_batch_item& it, int cap);
+int small_qr_launch(cudaStream_t st, const mak_batch_item* items, const int* which, int count,
+                    int positive, mak_info* infos, int cap);
 
 // Look-ahead (QR and Gauss-Jordan): a high-priority side stream factors the
 // next block while the main stream updates the far columns.  On/off for
