@@ -147,6 +147,8 @@ int mak_profile_read(int kind, double* total_ms, double* total_work, uint64_t* l
  *   MAK_SMALL_QR_BYTES     batched QR: blocks of at most this many bytes (m n
  *                          + 2 min(m,n) elements) are factored by the one-CTA
  *                          small-block kernel (0 = off; 200704)
+ *   MAK_SMALL_POLAR_BYTES  batched polar: the same for the one-CTA Newton
+ *                          iteration (0 = off; 200704)
  * mak_tuning_set: 0 ok, -1 unknown name, -2 value out of range; a NaN value
  * returns the parameter to its environment / default value.
  * mak_tuning_get: the value in effect.  mak_tuning_name(i): the i-th name,
@@ -382,6 +384,19 @@ int mak_batched_left_polar_workspace(const mak_batch_item* items, int nitems,
 int mak_batched_qr_compact_device(const mak_batch_item* items, int nitems,
                                   const mak_qr_opts* opts, mak_info* infos, mak_stream_t stream);
 int mak_small_qr_max_bytes(void);
+/* The same for left_polar! (PolarNewton, reference
+ * src/implementations/polar.jl:128-166): a block with m >= n whose m n +
+ * 2 n^2 + 2 n elements and n pivot indices fit mak_small_polar_max_bytes()
+ * runs the whole Newton iteration (QR of A when m > n, Gauss-Jordan inverses
+ * with partial pivoting, at most opts->maxiter steps, stopped at opts->tol or
+ * eps(real T)^(2/3)) in one CTA; mak_batched_left_polar sends such blocks to
+ * one persistent launch, mak_batched_left_polar_device takes a DEVICE work
+ * list (W in Q, P in R; infos[i].iterations / converged / singular as for a
+ * single call).  MAK_SMALL_POLAR_BYTES sets the limit (default 196 KiB). */
+int mak_batched_left_polar_device(const mak_batch_item* items, int nitems,
+                                  const mak_polar_opts* opts, mak_info* infos,
+                                  mak_stream_t stream);
+int mak_small_polar_max_bytes(void);
 int mak_batched_left_polar(const mak_batch_item* items, int nitems, const mak_polar_opts* opts,
                            void* work, size_t work_bytes, mak_info* infos, mak_stream_t stream);
 

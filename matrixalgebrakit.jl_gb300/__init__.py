@@ -51,12 +51,13 @@ __all__ += ["qr_pullback_", "left_polar_pullback_", "right_polar_pullback_", "qr
             "left_polar_pushforward_", "right_polar_pushforward_"]
 
 from .batched import (batch_items_device, batched_left_polar,  # noqa: E402
-                      batched_left_polar_pullback, batched_qr_compact, batched_qr_compact_device,
-                      batched_qr_pullback, small_qr_max_bytes)
+                      batched_left_polar_device, batched_left_polar_pullback, batched_qr_compact,
+                      batched_qr_compact_device, batched_qr_pullback, small_polar_max_bytes,
+                      small_qr_max_bytes)
 
 __all__ += ["batched_qr_compact", "batched_left_polar", "batched_qr_pullback",
             "batched_left_polar_pullback", "batched_qr_compact_device", "batch_items_device",
-            "small_qr_max_bytes"]
+            "small_qr_max_bytes", "batched_left_polar_device", "small_polar_max_bytes"]
 
 from .algorithms import RightOrthViaLQ, RightOrthViaPolar  # noqa: E402
 from .orthnull import (batched_left_orth, batched_project_isometric, left_null,  # noqa: E402

@@ -175,6 +175,9 @@ SIGNATURES["mak_batched_qr_compact"] = (C.c_int, [C.POINTER(mak_batch_item), C.c
 SIGNATURES["mak_batched_qr_compact_device"] = (C.c_int, [_p, C.c_int, C.POINTER(mak_qr_opts), _p,
                                                          _p])
 SIGNATURES["mak_small_qr_max_bytes"] = (C.c_int, [])
+SIGNATURES["mak_batched_left_polar_device"] = (C.c_int, [_p, C.c_int, C.POINTER(mak_polar_opts),
+                                                         _p, _p])
+SIGNATURES["mak_small_polar_max_bytes"] = (C.c_int, [])
 SIGNATURES["mak_batched_left_polar_workspace"] = (C.c_int, [C.POINTER(mak_batch_item), C.c_int,
                                                             C.POINTER(mak_polar_opts),
                                                             C.POINTER(_sz)])

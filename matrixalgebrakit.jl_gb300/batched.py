@@ -140,6 +140,55 @@ def batched_qr_compact_device(As, alg=None, copy_inputs=True, outs=None, items=N
     return outs
 
 
+def small_polar_max_bytes() -> int:
+    """Shared memory (bytes) a block may take in the one-CTA small-block
+    polar: m n + 2 n^2 + 2 n elements and n pivot indices (0: off)."""
+    return int(lib().mak_small_polar_max_bytes())
+
+
+def batched_left_polar_device(As, alg=None, copy_inputs=True, outs=None, items=None,
+                              _capturing=False, _info=None, **kwargs):
+    """left_polar of every block (m >= n) from a work list in DEVICE memory
+    (``mak_batched_left_polar_device``): one persistent launch in which each
+    CTA runs the whole Newton iteration of its blocks in shared memory;
+    every block must fit ``small_polar_max_bytes()``.  Returns [(W_i, P_i)];
+    ``_info`` (a list) receives the steps each block took."""
+    alg = select_algorithm("left_polar_", None, alg, **kwargs)
+    if not As:
+        return []
+    dev = As[0].device
+    for A in As:
+        check_cuda_tensor(A, "A")
+        if A.device != dev:
+            raise ArgumentError("all blocks must live on one device")
+        if A.shape[0] < A.shape[1]:
+            raise ArgumentError("every block needs at least as many rows as columns")
+    if outs is None:
+        outs = [(empty_cm(A.shape[0], A.shape[1], A.dtype, A.device),
+                 empty_cm(A.shape[1], A.shape[1], A.dtype, A.device)) for A in As]
+    work_As = [to_cm(A) for A in As] if copy_inputs else list(As)
+    if items is None:
+        items = batch_items_device(work_As, outs)
+    opts = _lib.mak_polar_opts(int(alg.maxiter), PRECISION_CODE[alg.precision],
+                               float(alg.tol) if alg.tol is not None else 0.0)
+    L = lib()
+    with torch.cuda.device(dev):
+        infos = torch.zeros(len(As) * INFO_BYTES, dtype=torch.uint8, device=dev)
+        rc = L.mak_batched_left_polar_device(items.data_ptr(), len(As), ct.byref(opts),
+                                             infos.data_ptr(), stream_handle(dev))
+        check_rc(rc, "mak_batched_left_polar_device")
+        if _capturing:
+            return outs
+        res = _read_infos(infos, len(As))
+    for i, inf in enumerate(res):
+        if inf.status != 0:
+            raise RuntimeError(f"mak_batched_left_polar_device: block {i}: device status "
+                               f"{inf.status}")
+    if _info is not None:
+        _info.extend((int(r.iterations), int(r.singular)) for r in res)
+    return outs
+
+
 def batched_left_polar(As, alg=None, copy_inputs=True, outs=None, _capturing=False, _info=None,
                        **kwargs):
     """left_polar of every block; returns [(W_i, P_i)].  Without host

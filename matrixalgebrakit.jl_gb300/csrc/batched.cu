@@ -114,12 +114,13 @@ static int plan(int kind, const mak_batch_item* items, int nitems, const void* o
   p.owner.assign(nitems, 0);
   p.ws_item.assign(nitems, 0);
   p.small.clear();
-  // QR blocks that fit one CTA's shared memory go to one persistent launch
-  const int small_cap = kind == BATCH_QR ? small_qr_cap() : 0;
+  // blocks that fit one CTA's shared memory go to one persistent launch
+  const int small_cap = kind == BATCH_QR ? small_qr_cap() : small_polar_cap();
   std::vector<int> order;
   order.reserve(nitems);
   for (int i = 0; i < nitems; i++) {
-    if (small_qr_fits(items[i], small_cap)) {
+    if (kind == BATCH_QR ? small_qr_fits(items[i], small_cap)
+                         : small_polar_fits(items[i], small_cap)) {
       p.owner[i] = -1;
       p.small.push_back(i);
       continue;
@@ -190,9 +191,15 @@ static int batched(int kind, const mak_batch_item* items, int nitems, const void
   if (!p.small.empty()) {
     // the small blocks: one persistent launch on the caller's stream, which
     // runs beside the internal streams (forked above, joined below)
-    const mak_qr_opts* o = (const mak_qr_opts*)opts;
-    rc_all = small_qr_launch(st, items, p.small.data(), (int)p.small.size(), o->positive, infos,
-                             small_qr_cap());
+    if (kind == BATCH_QR) {
+      const mak_qr_opts* o = (const mak_qr_opts*)opts;
+      rc_all = small_qr_launch(st, items, p.small.data(), (int)p.small.size(), o->positive,
+                               infos, small_qr_cap());
+    } else {
+      const mak_polar_opts* o = (const mak_polar_opts*)opts;
+      rc_all = small_polar_launch(st, items, p.small.data(), (int)p.small.size(), o->maxiter,
+                                  o->tol, infos, small_polar_cap());
+    }
   }
   {
     // the batch's streams already overlap the blocks (no look-ahead), and a

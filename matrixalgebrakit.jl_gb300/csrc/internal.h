@@ -64,6 +64,7 @@ enum TuneId {
   TUNE_LOOKAHEAD_TAIL_COLS,  // far columns from which down the side stream gets more SMs
   TUNE_LOOKAHEAD_TAIL_CTAS,  // the side stream's SMs in that tail
   TUNE_SMALL_QR_BYTES,       // batched QR: blocks up to this many bytes take the one-CTA kernel
+  TUNE_SMALL_POLAR_BYTES,    // batched polar: the same for the one-CTA polar kernel
   TUNE_COUNT
 };
 double tuning(int id);
@@ -76,6 +77,11 @@ int small_qr_cap();
 bool small_qr_fits(const mak_batch_item& it, int cap);
 int small_qr_launch(cudaStream_t st, const mak_batch_item* items, const int* which, int count,
                     int positive, mak_info* infos, int cap);
+// the same for the one-CTA left polar (PolarNewton), blocks with m >= n
+int small_polar_cap();
+bool small_polar_fits(const mak_batch_item& it, int cap);
+int small_polar_launch(cudaStream_t st, const mak_batch_item* items, const int* which, int count,
+                       int maxiter, double tol, mak_info* infos, int cap);
 
 // Look-ahead (QR and Gauss-Jordan): a high-priority side stream factors the
 // next block while the main stream updates the far columns.  On/off for

@@ -42,6 +42,7 @@ const Param kParams[TUNE_COUNT] = {
     {"MAK_LOOKAHEAD_TAIL_COLS", 4096, 0, 1073741824.0},
     {"MAK_LOOKAHEAD_TAIL_CTAS", 96, 8, 144},
     {"MAK_SMALL_QR_BYTES", 200704, 0, 229376},
+    {"MAK_SMALL_POLAR_BYTES", 200704, 0, 229376},
 };
 
 std::atomic<double> g_set[TUNE_COUNT];

@@ -1,7 +1,8 @@
-"""GPU tests of the one-CTA small-block QR (csrc/small.cu): blocks factored
-in shared memory by one persistent launch over a work list -- in DEVICE
-memory (mak_batched_qr_compact_device) or taken by the batched driver --
-each compared with the CPU oracle's qr_compact (positive gauge)."""
+"""GPU tests of the one-CTA small-block QR and polar (csrc/small.cu): blocks
+factored in shared memory by one persistent launch over a work list -- in
+DEVICE memory (mak_batched_qr_compact_device / mak_batched_left_polar_device)
+or taken by the batched driver -- each compared with the CPU oracle's
+qr_compact (positive gauge) and left_polar_newton / left_polar_svd."""
 
 from __future__ import annotations
 
@@ -130,3 +131,63 @@ def test_small_qr_graph_capture(mak, cuda):
     torch.cuda.synchronize()
     for A, (Q, R) in zip(blocks, outs):
         assert O.rel_err(to_host(R), O.qr_compact(A)[1]) <= 1e-12
+
+
+POLAR_SHAPES = [(1, 1), (5, 1), (7, 3), (40, 40), (64, 17), (100, 48), (130, 31), (33, 33)]
+
+
+@pytest.mark.parametrize("dt", DTYPES, ids=lambda d: np.dtype(d).name)
+def test_small_polar_device_list(mak, cuda, dt):
+    rng = np.random.default_rng(91)
+    blocks = [O.gaussian(rng, m, n, dt) for (m, n) in POLAR_SHAPES]
+    steps = []
+    outs = mak.batched_left_polar_device([to_dev(A, cuda) for A in blocks], _info=steps)
+    dbl = dt in (np.float64, np.complex128)
+    for A, (W, P), (k, sing) in zip(blocks, outs, steps):
+        Wh, Ph = to_host(W), to_host(P)
+        n = A.shape[1]
+        assert sing == 0
+        assert np.array_equal(Ph, Ph.conj().T)  # exactly Hermitian
+        back = np.linalg.norm(A - Wh @ Ph) / np.linalg.norm(A)
+        assert back <= (1e-12 if dbl else 2e-5), (A.shape, back)
+        assert O.orth_error(Wh) <= (1e-12 if dbl else 2e-5) * np.sqrt(n)
+        Wo, Po = O.left_polar_svd(A.astype(np.complex128 if np.iscomplexobj(A) else np.float64))
+        assert O.rel_err(Wh, Wo) <= (1e-9 if dbl else 1e-3), A.shape
+        if dbl:
+            ko = O.left_polar_newton(A)[2]["iterations"]
+            assert abs(k - ko) <= 1, (A.shape, k, ko)
+
+
+def test_small_polar_ill_conditioned_and_singular(mak, cuda):
+    """kappa = 1e6 (several Newton steps) and an exactly singular block (a
+    zero column: the Gauss-Jordan inverse meets a zero pivot)."""
+    rng = np.random.default_rng(92)
+    n = 40
+    U = np.linalg.qr(rng.standard_normal((96, n)))[0]
+    V = np.linalg.qr(rng.standard_normal((n, n)))[0]
+    A = np.asfortranarray((U * np.logspace(0, -6, n)[None, :]) @ V.T)
+    S = O.gaussian(rng, 50, 10, np.float64)
+    S[:, 4] = 0.0
+    steps = []
+    outs = mak.batched_left_polar_device([to_dev(A, cuda), to_dev(S, cuda)], _info=steps)
+    Wh, Ph = to_host(outs[0][0]), to_host(outs[0][1])
+    assert np.linalg.norm(A - Wh @ Ph) / np.linalg.norm(A) <= 1e-12
+    assert O.orth_error(Wh) <= 1e-12 * np.sqrt(n)
+    ko = O.left_polar_newton(A)[2]["iterations"]
+    assert abs(steps[0][0] - ko) <= 1 and steps[0][1] == 0
+    assert steps[1][1] == 1  # singular reported in the record
+
+
+def test_batched_polar_routes_small_blocks(mak, cuda):
+    """The batched polar sends the blocks that fit to the one-CTA launch and
+    the others to its streams; every block meets the reference's accuracy."""
+    rng = np.random.default_rng(93)
+    shapes = [(20, 10), (600, 300), (64, 64), (700, 350), (5, 3), (256, 40)]
+    blocks = [O.gaussian(rng, m, n, np.float64 if i % 2 else np.complex128)
+              for i, (m, n) in enumerate(shapes)]
+    for prec in ("native", "mixed"):
+        outs = mak.batched_left_polar([to_dev(A, cuda) for A in blocks], precision=prec)
+        for A, (W, P) in zip(blocks, outs):
+            Wh, Ph = to_host(W), to_host(P)
+            assert np.linalg.norm(A - Wh @ Ph) / np.linalg.norm(A) <= 1e-12
+            assert O.orth_error(Wh) <= 1e-12 * np.sqrt(A.shape[1])
