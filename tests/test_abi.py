@@ -4,6 +4,8 @@ without a GPU (no compute calls)."""
 
 from __future__ import annotations
 
+import os
+
 import ctypes as C
 import re
 from pathlib import Path
@@ -234,6 +236,32 @@ def test_tuning_table_is_host_only(mak):
     lib = mak.library()
     assert lib.mak_tuning_set(b"MAK_BATCH_STREAMS", math.nan) == 0
     assert lib.mak_tuning_name(len(names)) is None
+
+
+def test_tuning_switches_and_defaults(mak):
+    """The kernel switches and launch-shape parameters are in the table with
+    their built-in defaults (no environment override in this process) and
+    range checks."""
+    from mak_gb300 import autotune
+
+    defaults = {"MAK_PANEL_PAIR": 1, "MAK_OZ_MERGED": 1, "MAK_OZ_NARROW": 1,
+                "MAK_LOOKAHEAD_CTAS": 48, "MAK_LOOKAHEAD_TAIL_COLS": 4096,
+                "MAK_LOOKAHEAD_TAIL_CTAS": 96, "MAK_SMALL_QR_BYTES": 200704,
+                "MAK_SMALL_POLAR_BYTES": 200704, "MAK_PANEL_HIER_C": 0}
+    for name, value in defaults.items():
+        if name in os.environ:
+            continue
+        assert autotune.get_tuning(name) == value, name
+    for name, bad in (("MAK_PANEL_PAIR", 2), ("MAK_OZ_NARROW", -1),
+                      ("MAK_LOOKAHEAD_TAIL_CTAS", 200), ("MAK_SMALL_QR_BYTES", 1 << 20)):
+        with pytest.raises(ValueError):
+            autotune.set_tuning({name: bad})
+    autotune.set_tuning(MAK_PANEL_PAIR=0, MAK_SMALL_QR_BYTES=0)
+    try:
+        assert autotune.get_tuning("MAK_PANEL_PAIR") == 0
+        assert autotune.get_tuning("MAK_SMALL_QR_BYTES") == 0
+    finally:
+        autotune.reset_tuning(["MAK_PANEL_PAIR", "MAK_SMALL_QR_BYTES"])
 
 
 def test_tuning_table_json_round_trip(mak, tmp_path):
