@@ -149,6 +149,9 @@ int mak_profile_read(int kind, double* total_ms, double* total_work, uint64_t* l
  *                          small-block kernel (0 = off; 200704)
  *   MAK_SMALL_POLAR_BYTES  batched polar: the same for the one-CTA Newton
  *                          iteration (0 = off; 200704)
+ *   MAK_QR_PANEL_SPLIT     mixed QR: a 32-wide panel's update of the rest of
+ *                          its 128-wide block as split tensor-core products
+ *                          (1), or on the FP64 pipe (0)
  * mak_tuning_set: 0 ok, -1 unknown name, -2 value out of range; a NaN value
  * returns the parameter to its environment / default value.
  * mak_tuning_get: the value in effect.  mak_tuning_name(i): the i-th name,

@@ -65,6 +65,7 @@ enum TuneId {
   TUNE_LOOKAHEAD_TAIL_CTAS,  // the side stream's SMs in that tail
   TUNE_SMALL_QR_BYTES,       // batched QR: blocks up to this many bytes take the one-CTA kernel
   TUNE_SMALL_POLAR_BYTES,    // batched polar: the same for the one-CTA polar kernel
+  TUNE_QR_PANEL_SPLIT,       // mixed QR: within-block panel updates as split products (1)
   TUNE_COUNT
 };
 double tuning(int id);

@@ -1059,15 +1059,27 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     }
     ozs = ar.take<char>(oz_bytes);
   }
-  // the block Gram matrix runs on the look-ahead stream: its own scratch
+  // the block Gram matrix and the within-block updates of the panels run on
+  // the look-ahead stream: their own scratch, and (mixed) W / T^H W of a
+  // panel's update
   size_t gram_bytes = 0;
   char* grams = nullptr;
+  T *Wp = nullptr, *W2p = nullptr;
+  const bool panel_split = mixed && tuning(TUNE_QR_PANEL_SPLIT) != 0;
   if (mixed) {
-    Arena meas(nullptr, 0);
-    gemm_prec<T>(st, precision, NBO, NBO, m, one_<T>(), opnd<T>(nullptr, 1),
-                 opnd<T>(nullptr, 1), zero_<T>(), nullptr, 1, meas, nullptr);
-    gram_bytes = meas.off + 1024;
+    const int64_t shapes[3][3] = {{NBO, NBO, m}, {NBMAX, NBO, m}, {m, NBO, NBMAX}};
+    for (int q = 0; q < (panel_split ? 3 : 1); q++) {
+      Arena meas(nullptr, 0);
+      gemm_prec<T>(st, precision, shapes[q][0], shapes[q][1], shapes[q][2], one_<T>(),
+                   opnd<T>(nullptr, 1), opnd<T>(nullptr, 1), zero_<T>(), nullptr, 1, meas,
+                   nullptr);
+      if (meas.off + 1024 > gram_bytes) gram_bytes = meas.off + 1024;
+    }
     grams = ar.take<char>(gram_bytes);
+    if (panel_split) {
+      Wp = ar.take<T>((size_t)NBMAX * NBO);
+      W2p = ar.take<T>((size_t)NBMAX * NBO);
+    }
   }
   if (ar.base == nullptr) return 0;
   if (!ar.ok()) return MAK_ERR_WORKSPACE;
@@ -1118,6 +1130,33 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     return gemm<T>(s, mp, nt, jb, -one_<T>(), opnd<T>(Ap, lda, OP_N, MASK_UNIT_LOWER),
                    opnd<T>(W2, jb), one_<T>(), C, lda);
   };
+  // mixed: a 32-wide panel's reflector applied to the rest of its 128-wide
+  // block with split products (W = V^H C, W2 = T^H W, C -= V W2) on the
+  // side stream's scratch; gemm_prec keeps products below the split gate
+  // native
+  auto larfb_panel_split = [&](int64_t j0, int jb, const T* Tb, int64_t c0, int64_t c1,
+                               cudaStream_t s) -> int {
+    const int64_t nt = c1 - c0;
+    if (nt <= 0) return 0;
+    const int64_t mp = m - j0;
+    const T* Ap = A + j0 + j0 * lda;
+    T* C = A + j0 + c0 * lda;
+    const int mc = s == st ? 0 : tl_side_ctas;
+    {
+      Arena ga(grams, gram_bytes);
+      MAK_TRY(gemm_prec<T>(s, precision, jb, nt, mp, one_<T>(),
+                           opnd<T>(Ap, lda, OP_C, MASK_UNIT_LOWER), opnd<T>(C, lda), zero_<T>(),
+                           Wp, jb, ga, status, mc));
+    }
+    note_launch();
+    reduce_trmm_kernel<T><<<(unsigned)ceil_div(nt, 32), 256, 0, s>>>(jb, (int)nt, 1, Wp,
+                                                                      (int64_t)jb * nt, Tb, 1, W2p);
+    MAK_CUDA_TRY(cudaGetLastError());
+    Arena ga(grams, gram_bytes);
+    return gemm_prec<T>(s, precision, mp, nt, jb, -one_<T>(),
+                        opnd<T>(Ap, lda, OP_N, MASK_UNIT_LOWER), opnd<T>(W2p, jb), one_<T>(), C,
+                        lda, ga, status, mc);
+  };
   // one 32-wide panel (cooperative launch)
   // on the look-ahead stream the panel takes a few SMs only, leaving the
   // rest to the trailing GEMM it overlaps with
@@ -1164,7 +1203,10 @@ int qr_run(cudaStream_t st, int64_t m, int64_t n, T* A, int64_t lda, T* Q, int64
     for (int64_t j0 = J0; j0 < J0 + JB; j0 += nb) {
       const int jb = (int)((J0 + JB - j0) < nb ? (J0 + JB - j0) : nb);
       MAK_TRY(panel(j0, jb, s));
-      MAK_TRY(larfb_native(j0, jb, Ts + (j0 / nb) * NBMAX * NBMAX, j0 + jb, J0 + JB, s));
+      if (panel_split)
+        MAK_TRY(larfb_panel_split(j0, jb, Ts + (j0 / nb) * NBMAX * NBMAX, j0 + jb, J0 + JB, s));
+      else
+        MAK_TRY(larfb_native(j0, jb, Ts + (j0 / nb) * NBMAX * NBMAX, j0 + jb, J0 + JB, s));
     }
     if (!mixed) return 0;
     const T* V = A + J0 + J0 * lda;

@@ -43,6 +43,7 @@ const Param kParams[TUNE_COUNT] = {
     {"MAK_LOOKAHEAD_TAIL_CTAS", 96, 8, 144},
     {"MAK_SMALL_QR_BYTES", 200704, 0, 229376},
     {"MAK_SMALL_POLAR_BYTES", 200704, 0, 229376},
+    {"MAK_QR_PANEL_SPLIT", 1, 0, 1},
 };
 
 std::atomic<double> g_set[TUNE_COUNT];

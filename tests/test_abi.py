@@ -247,7 +247,8 @@ def test_tuning_switches_and_defaults(mak):
     defaults = {"MAK_PANEL_PAIR": 1, "MAK_OZ_MERGED": 1, "MAK_OZ_NARROW": 1,
                 "MAK_LOOKAHEAD_CTAS": 48, "MAK_LOOKAHEAD_TAIL_COLS": 4096,
                 "MAK_LOOKAHEAD_TAIL_CTAS": 96, "MAK_SMALL_QR_BYTES": 200704,
-                "MAK_SMALL_POLAR_BYTES": 200704, "MAK_PANEL_HIER_C": 0}
+                "MAK_SMALL_POLAR_BYTES": 200704, "MAK_PANEL_HIER_C": 0,
+                "MAK_QR_PANEL_SPLIT": 1}
     for name, value in defaults.items():
         if name in os.environ:
             continue
